@@ -1,0 +1,194 @@
+/*
+ * patchmatch_gb300.h -- C ABI of the GB300-native PatchMatch multi-view-stereo engine.
+ *
+ * This is the drop-in boundary for the hot path of yhsa678/patchMatch_cuda: one depth
+ * map (and the sampled view-selection map) for one reference image from N calibrated
+ * source views, by row-sweep PatchMatch propagation with homography-warped windowed NCC
+ * and HMM view selection. Plain pointers and sizes only; every entry point returns a
+ * pm_status and never exits the process. Handles hold no process-global state, so
+ * several handles may run concurrently (each owns a CUDA stream). A single handle is not
+ * thread-safe.
+ *
+ * Reference interface each entry point replaces (paths relative to the reference root):
+ *   pm_create             PatchMatch::PatchMatch        src/patchMatch.h:71-72, src/patchMatch.cu:132-206
+ *   pm_run                PatchMatch::runPatchMatch     src/patchMatch.h:74,    src/patchMatch.cu:263-407
+ *   pm_get_depth          Array2D_wrapper::copyData     src/array2d_wrapper.h:37-47 (on _depthMap)
+ *   pm_get_view_selection _usedImgsID (never read back by the reference)  src/patchMatch.cu:170, :381-385
+ *   pm_save_depth         Array2D_wrapper::saveToFile   src/array2d_wrapper.h:51-70
+ *   pm_destroy            PatchMatch::~PatchMatch       src/patchMatch.cu:208-234
+ *   pm_run_batch          (no counterpart: several references in one launch per sweep)
+ * Lower-level entry points expose single stages for parity checks and for callers that
+ * drive their own schedule; each names its reference counterpart below.
+ */
+#ifndef PATCHMATCH_GB300_H
+#define PATCHMATCH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum pm_status {
+    PM_OK = 0,
+    PM_ERR_INVALID_ARGUMENT = 1,
+    PM_ERR_WINDOW_SIZE = 2,      /* half window outside [1, 22] (patchMatch.cu:265-270,
+                                    array2d_refImg.cu:71-97)                            */
+    PM_ERR_TOO_FEW_VIEWS = 3,    /* fewer than 2 images (patchMatch.cu:137-142)          */
+    PM_ERR_TOO_MANY_VIEWS = 4,   /* more than PM_MAX_SOURCE_VIEWS source views            */
+    PM_ERR_IMAGE = 5,            /* missing, empty or oversized image                     */
+    PM_ERR_CAMERA = 6,           /* singular or non-finite K / R / t                      */
+    PM_ERR_CUDA = 7,             /* a CUDA runtime call failed                            */
+    PM_ERR_OUT_OF_MEMORY = 8,
+    PM_ERR_IO = 9,
+    PM_ERR_NO_DEVICE = 10,
+    PM_ERR_STATE = 11,           /* call out of order (e.g. view selection before a run)  */
+    PM_ERR_UNSUPPORTED = 12
+} pm_status;
+
+#define PM_MAX_SOURCE_VIEWS 32
+#define PM_MAX_HALF_WINDOW 22
+
+typedef enum pm_prefilter_mode {
+    PM_PREFILTER_NONE = 0,      /* what the reference runtime does (GaussianBlurCUDA is never called) */
+    PM_PREFILTER_BOX = 1,       /* GaussianBlurCUDA as written: box of width max(5, odd(5 sigma))     */
+    PM_PREFILTER_GAUSSIAN = 2   /* the normalised Gaussian weights that class computes first          */
+} pm_prefilter_mode;
+
+typedef enum pm_precision {
+    PM_PRECISION_FP32 = 0,      /* FP32 texels (u8 texels when unfiltered: the same values)  */
+    PM_PRECISION_MIXED = 1      /* FP16 texels, shifted window moments, FP64 window origin    */
+} pm_precision;
+
+typedef enum pm_init_mode {
+    PM_INIT_RANDOM = 0          /* uniform depth in [near, far) (array2d_wrapper.cu:3-20)      */
+} pm_init_mode;
+
+typedef enum pm_direction {     /* sweep order within one iteration (patchMatch.cu:344-391) */
+    PM_DIR_LEFT_TO_RIGHT = 0,
+    PM_DIR_TOP_TO_BOTTOM = 1,
+    PM_DIR_RIGHT_TO_LEFT = 2,
+    PM_DIR_BOTTOM_TO_TOP = 3
+} pm_direction;
+
+/* One calibrated grayscale view (Image::updateCamParam, image.cpp:39-61): projection
+ * K [R | t], pixel ~ K (R X + t). The engine copies the pixels at pm_create. */
+typedef struct pm_view {
+    const uint8_t *gray;        /* height rows of width bytes                                */
+    int width, height;
+    int stride;                 /* bytes between rows (>= width)                             */
+    float K[9], R[9], t[3];     /* row-major                                                 */
+} pm_view;
+
+/* The PatchMatch constructor's parameters (patchMatch.h:71-72) and main.cpp's INI keys
+ * (main.cpp:47-85), plus the engine's own knobs. pm_default_params fills the defaults. */
+typedef struct pm_params {
+    float depth_near, depth_far;   /* depthRangeNear / depthRangeFar                         */
+    int half_window;               /* halfWindowSize, 1..22                                  */
+    int num_samples;               /* numOfSamples (views sampled per pixel, >= 1)           */
+    float sp_alpha;                /* SPMAlpha                                               */
+    float gaussian_sigma;          /* gaussianSigma (prefilter width)                        */
+    int prefilter;                 /* pm_prefilter_mode                                      */
+    int num_iterations;            /* numOfIterations                                        */
+    float orientation_x;           /* orientationX (plane normal x; default 0)               */
+    float orientation_z;           /* orientationZ (plane normal z; default 1)               */
+    uint64_t seed;                 /* Philox key                                             */
+    int precision;                 /* pm_precision                                           */
+    int init_mode;                 /* pm_init_mode                                           */
+    int threads_per_line;          /* 0 = tuned; else 32, 64 or 128                          */
+    int quirks;                    /* 1 (default): keep the reference's leading-edge window
+                                      misalignment (patchMatch.cu:546); 0: aligned windows   */
+    int gpu_id;                    /* gpuId: -1 = current device (main.cpp:56-59)            */
+    int block_dim_x, block_dim_y;  /* accepted for signature parity, unused                  */
+} pm_params;
+
+typedef struct pm_handle pm_handle;
+
+typedef struct pm_stats {
+    unsigned long long cost_evals;       /* NCC evaluations the algorithm performed       */
+    unsigned long long cost_evals_done;  /* evaluations actually computed (cache hits are
+                                            reused results)                               */
+    float ms_prepare;                    /* pm_create device work                         */
+    float ms_init;                       /* last run: depth init + initial costs          */
+    float ms_sweeps;                     /* last run: all sweeps                          */
+    float ms_total;                      /* last run                                      */
+    int threads_per_line;                /* chosen by the tuner or the caller             */
+    int texel_bytes;                     /* 1 (u8), 2 (fp16) or 4 (fp32)                  */
+} pm_stats;
+
+void pm_default_params(pm_params *p);
+const char *pm_status_string(pm_status s);
+const char *pm_last_error(const pm_handle *h);
+
+/* Validates, sets up cameras (K^-1, C, H1, H2 in FP64), uploads and prefilters the images,
+ * builds source textures and the reference-window moments. ref_id indexes views. */
+pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_params *p,
+                    pm_handle **out);
+pm_status pm_destroy(pm_handle *h);
+
+/* Initial depth + every view's cost, then num_iterations x 4 sweeps. Synchronous. */
+pm_status pm_run(pm_handle *h);
+/* Same work enqueued on the handle's stream (captured once as a CUDA graph). */
+pm_status pm_run_async(pm_handle *h);
+pm_status pm_synchronize(pm_handle *h);
+/* Runs several handles with one launch per sweep for all of them (handles grouped by
+ * window size); synchronous. */
+pm_status pm_run_batch(pm_handle *const *hs, int n);
+
+/* Results. dst_pitch in bytes (0 = width * sizeof(float)). */
+pm_status pm_get_depth(pm_handle *h, float *dst, size_t dst_pitch);
+/* num_samples layers of height*width bytes: layer j, row y, column x holds the view
+ * sampled for sample j at (x, y) in the final bottom-to-top sweep (255: none). */
+pm_status pm_get_view_selection(pm_handle *h, uint8_t *dst);
+/* "<W>&<H>&1&" then raw float32 row-major depth (array2d_wrapper.h:51-70). */
+pm_status pm_save_depth(pm_handle *h, const char *path);
+
+pm_status pm_get_stats(const pm_handle *h, pm_stats *out);
+/* The handle's cudaStream_t, for callers that time or order work around it. */
+pm_status pm_get_stream(const pm_handle *h, void **stream);
+pm_status pm_get_size(const pm_handle *h, int *width, int *height, int *n_src);
+
+/* ---- single stages (parity checks, custom schedules) ---------------------------------- */
+/* generate_kernel_float (array2d_wrapper.cu:3-20) into the depth map. */
+pm_status pm_init_depth(pm_handle *h);
+/* computeAllCostGivenDepth (patchMatch.cu:775-816): all costs at the current depth;
+ * axis 1 pairs windows like the reference's transposed layout, axis 0 like vertical sweeps. */
+pm_status pm_compute_costs(pm_handle *h, int axis);
+/* One sweep, topToDown / downToTop (patchMatch.cu:818-1209). sweep_id keys the random
+ * draws; record_views writes the view-selection map. */
+pm_status pm_run_sweep(pm_handle *h, int direction, uint32_t sweep_id, int num_samples,
+                       int record_views);
+pm_status pm_set_depth(pm_handle *h, const float *src);
+/* Costs are pixel-major: (y * width + x) * n_src + view. */
+pm_status pm_get_costs(pm_handle *h, float *dst);
+pm_status pm_set_costs(pm_handle *h, const float *src);
+/* Reference-window box sums (array2d_refImg.cu:11-67) and the reference texels. */
+pm_status pm_get_ref_maps(pm_handle *h, float *ref, float *sum_i, float *sum_ii);
+/* Source texels as stored for sampling (after prefilter and precision rounding). */
+pm_status pm_get_source_texels(pm_handle *h, int view, float *dst);
+/* computeNCC (patchMatch.cu:433-611) for n (x, y, view, depth, axis) tuples. */
+pm_status pm_eval_costs(pm_handle *h, int n, const int *xs, const int *ys, const int *views,
+                        const float *depths, const int *axes, float *out);
+/* Bilinear source fetch of patchMatch.cu:543 at source coordinates (xs, ys). */
+pm_status pm_sample_source(pm_handle *h, int view, int n, const float *xs, const float *ys,
+                           float *out);
+
+/* ---- direction flip ---------------------------------------------------------------------
+ * cudaTranspose::transpose2dData (cudaTranspose.h:9-71) over `layers` stacked layers of
+ * DEVICE memory: layer l of the input is rows [l*height, (l+1)*height) of a width-wide
+ * pitched float image; the output layer is height wide and width tall. The engine's sweeps
+ * address both directions in place and never need it; it serves callers that hold maps in
+ * the reference's stacked layout. stream may be NULL. */
+pm_status pm_transpose_layers(const float *d_in, size_t in_pitch, float *d_out,
+                              size_t out_pitch, int width, int height, int layers,
+                              void *stream);
+
+/* ---- Philox draws (array2d_psng replacement) -------------------------------------------
+ * Device-side Philox4x32-10 for n counters; out gets 4 words per counter. */
+pm_status pm_philox(uint64_t seed, int n, const uint32_t *counters, uint32_t *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,103 @@
+/*
+ * pm_oracle.h -- CPU restatement of the PatchMatch multi-view-stereo hot path of
+ * yhsa678/patchMatch_cuda (TEST INFRASTRUCTURE ONLY).
+ *
+ * This oracle is the checker for the CUDA engine in patchmatch_cuda_gb300/. Only the
+ * tests, the smoke entry point and the CPU-baseline legs of bench.py may load it. The
+ * product path never calls it.
+ *
+ * Parity status: unpinned by the reference. yhsa678/patchMatch_cuda ships no tests,
+ * fixtures or golden vectors, and its own code cannot be built here (it needs CUDA
+ * texture references, which CUDA 12 removed, plus OpenCV and Boost). The restatement is
+ * pinned instead by known-answer tests derived from the reference code (identical
+ * windows -> 0, flat window -> 1, window outside the source -> 2, tie rule, message
+ * fixed points, sampling of a one-hot CDF) and by the ground truth of seeded synthetic
+ * scenes.
+ *
+ * Numbers: built with real = double (the FP64 oracle) or, with -DPMO_REAL_FLOAT, with
+ * real = float (the timed CPU baseline). The API always passes double arrays.
+ */
+#ifndef PM_ORACLE_H
+#define PM_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Sweep directions, in the order the reference schedules them within one iteration
+ * (patchMatch.cu:344-391). LR and RL run on the transposed maps in the reference
+ * (isRotated = true). */
+enum { PMO_DIR_LR = 0, PMO_DIR_TB = 1, PMO_DIR_RL = 2, PMO_DIR_BT = 3 };
+
+/* Purposes of random draws. A draw is keyed by (pixel, sweep, purpose, sub-index), so
+ * every draw of the reference's per-thread curand stream maps to one Philox counter. */
+enum {
+    PMO_RNG_INIT = 1,      /* initial depth, array2d_wrapper.cu:15                     */
+    PMO_RNG_BWD = 2,       /* cost==2 replacement in computeMessageBackward (:680-682)  */
+    PMO_RNG_FWD_PRE = 3,   /* same, forward message with the old costs (:905)           */
+    PMO_RNG_FWD_POST = 4,  /* same, forward message with the new costs (:874, :999)     */
+    PMO_RNG_RAND_DEPTH = 5,/* random depth hypothesis (:937)                           */
+    PMO_RNG_SAMPLE = 6     /* view sample j (:942)                                      */
+};
+
+typedef struct pmo_problem {
+    int width, height;              /* reference image size                               */
+    int n_src;                      /* number of source views                             */
+    int half_window;                /* halfWindowSize, window side = 2*hw+1               */
+    const float *ref;               /* height*width reference texels (u8/255 or filtered) */
+    const float *const *src;        /* n_src source images, row-major texels               */
+    const int *src_width;
+    const int *src_height;
+    const double *hh;               /* n_src*18: H1 (row-major 3x3) then H2, image.cpp:4-13 */
+    double inv_k[4];                /* K^-1 (0,0), (0,2), (1,1), (1,2), patchMatch.cu:155-156 */
+    double orientation[3];          /* plane normal (orientationX, 0, orientationZ)        */
+    double depth_near, depth_far;
+    float sp_alpha;                 /* SPMAlpha; squared in float as at patchMatch.cu:316  */
+    uint64_t seed;
+    uint32_t batch_id;              /* fourth Philox counter word                          */
+    int quirks;                     /* nonzero: keep the reference's ref/source window
+                                       misalignment at the leading edge (:546)            */
+} pmo_problem;
+
+void pmo_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+double pmo_uniform(uint64_t seed, uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3);
+
+void pmo_init_relative(const double k_ref[9], const double r_ref[9], const double t_ref[3],
+                       const double k_src[9], const double r_src[9], const double t_src[3],
+                       double orientation_x, double orientation_z,
+                       double out_hh[18], double out_inv_k[4]);
+
+int pmo_prefilter(const float *in, int width, int height, int mode, float sigma, float *out);
+void pmo_box_moments(const float *img, int width, int height, int half_window,
+                     double *sum_i, double *sum_ii);
+
+double pmo_ncc(const pmo_problem *p, const double *sum_i, const double *sum_ii,
+               int x, int y, int view, double depth, int axis);
+void pmo_ncc_batch(const pmo_problem *p, const double *sum_i, const double *sum_ii, int n,
+                   const int *xs, const int *ys, const int *views, const double *depths,
+                   const int *axes, double *out);
+
+void pmo_init_depth(const pmo_problem *p, double *depth);
+long long pmo_initial_costs(const pmo_problem *p, const double *sum_i, const double *sum_ii,
+                            const double *depth, double *cost);
+long long pmo_sweep(const pmo_problem *p, const double *sum_i, const double *sum_ii,
+                    double *depth, double *cost, int dir, uint32_t sweep_id, int num_samples,
+                    unsigned char *view_sel, int line_begin, int line_end);
+long long pmo_run(const pmo_problem *p, int iterations, int num_samples,
+                  const double *sum_i, const double *sum_ii,
+                  double *depth, double *cost, unsigned char *view_sel);
+
+/* Message updates and the tie rule, exposed for known-answer tests. */
+double pmo_msg_forward(double msg, double cost, double u_if_two, float sp_alpha);
+double pmo_msg_backward(double msg, double cost, double u_if_two, float sp_alpha);
+int pmo_find_min_cost(const double cost[3]);
+
+int pmo_num_threads(void);
+int pmo_real_bytes(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

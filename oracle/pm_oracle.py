@@ -1,0 +1,240 @@
+"""ctypes wrapper of the CPU oracle (pm_oracle.c). TEST INFRASTRUCTURE ONLY.
+
+`Oracle(problem_inputs, fp32=False)` holds one problem: reference texels, source texels,
+homographies (double), K^-1 terms, parameters. Parity status: unpinned by the reference (it
+ships no tests or fixtures and cannot be built here); pinned by code-derived known-answer
+tests and synthetic ground truth.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+BUILD = HERE / "_build"
+
+DIR_LR, DIR_TB, DIR_RL, DIR_BT = 0, 1, 2, 3
+RNG_INIT, RNG_BWD, RNG_FWD_PRE, RNG_FWD_POST, RNG_RAND_DEPTH, RNG_SAMPLE = 1, 2, 3, 4, 5, 6
+
+
+def build() -> None:
+    r = subprocess.run(["make", "-s", "-C", str(HERE)], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
+
+
+class _Problem(C.Structure):
+    _fields_ = [
+        ("width", C.c_int), ("height", C.c_int), ("n_src", C.c_int), ("half_window", C.c_int),
+        ("ref", C.c_void_p), ("src", C.c_void_p), ("src_width", C.c_void_p), ("src_height", C.c_void_p),
+        ("hh", C.c_void_p), ("inv_k", C.c_double * 4), ("orientation", C.c_double * 3),
+        ("depth_near", C.c_double), ("depth_far", C.c_double), ("sp_alpha", C.c_float),
+        ("seed", C.c_uint64), ("batch_id", C.c_uint32), ("quirks", C.c_int),
+    ]
+
+
+_libs: dict[bool, C.CDLL] = {}
+
+
+def load(fp32: bool = False) -> C.CDLL:
+    if fp32 in _libs:
+        return _libs[fp32]
+    path = BUILD / ("liboracle_f32.so" if fp32 else "liboracle_f64.so")
+    if not path.exists():
+        build()
+    lib = C.CDLL(str(path))
+    P = C.c_void_p
+    lib.pmo_philox4x32_10.argtypes = [P, P, P]
+    lib.pmo_uniform.restype = C.c_double
+    lib.pmo_uniform.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32]
+    lib.pmo_init_relative.argtypes = [P, P, P, P, P, P, C.c_double, C.c_double, P, P]
+    lib.pmo_prefilter.restype = C.c_int
+    lib.pmo_prefilter.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_float, P]
+    lib.pmo_box_moments.argtypes = [P, C.c_int, C.c_int, C.c_int, P, P]
+    lib.pmo_ncc.restype = C.c_double
+    lib.pmo_ncc.argtypes = [P, P, P, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int]
+    lib.pmo_ncc_batch.argtypes = [P, P, P, C.c_int, P, P, P, P, P, P]
+    lib.pmo_init_depth.argtypes = [P, P]
+    lib.pmo_initial_costs.restype = C.c_longlong
+    lib.pmo_initial_costs.argtypes = [P, P, P, P, P]
+    lib.pmo_sweep.restype = C.c_longlong
+    lib.pmo_sweep.argtypes = [P, P, P, P, P, C.c_int, C.c_uint32, C.c_int, P, C.c_int, C.c_int]
+    lib.pmo_run.restype = C.c_longlong
+    lib.pmo_run.argtypes = [P, C.c_int, C.c_int, P, P, P, P, P]
+    lib.pmo_msg_forward.restype = C.c_double
+    lib.pmo_msg_forward.argtypes = [C.c_double, C.c_double, C.c_double, C.c_float]
+    lib.pmo_msg_backward.restype = C.c_double
+    lib.pmo_msg_backward.argtypes = [C.c_double, C.c_double, C.c_double, C.c_float]
+    lib.pmo_find_min_cost.restype = C.c_int
+    lib.pmo_find_min_cost.argtypes = [P]
+    lib.pmo_num_threads.restype = C.c_int
+    lib.pmo_real_bytes.restype = C.c_int
+    _libs[fp32] = lib
+    return lib
+
+
+def philox(counter, key) -> np.ndarray:
+    lib = load()
+    c = np.ascontiguousarray(counter, np.uint32)
+    k = np.ascontiguousarray(key, np.uint32)
+    out = np.zeros(4, np.uint32)
+    lib.pmo_philox4x32_10(c.ctypes.data, k.ctypes.data, out.ctypes.data)
+    return out
+
+
+def uniform(seed: int, c0: int, c1: int, c2: int, c3: int = 0) -> float:
+    return load().pmo_uniform(seed, c0, c1, c2, c3)
+
+
+def init_relative(K_ref, R_ref, t_ref, K_src, R_src, t_src, nx=0.0, nz=1.0):
+    lib = load()
+    arrs = [np.ascontiguousarray(a, np.float64).ravel() for a in (K_ref, R_ref, t_ref, K_src, R_src, t_src)]
+    hh = np.zeros(18)
+    ik = np.zeros(4)
+    lib.pmo_init_relative(*[a.ctypes.data for a in arrs], nx, nz, hh.ctypes.data, ik.ctypes.data)
+    return hh, ik
+
+
+def prefilter(img: np.ndarray, mode: int, sigma: float, fp32: bool = False) -> np.ndarray:
+    lib = load(fp32)
+    a = np.ascontiguousarray(img, np.float32)
+    out = np.empty_like(a)
+    if lib.pmo_prefilter(a.ctypes.data, a.shape[1], a.shape[0], mode, sigma, out.ctypes.data) != 0:
+        raise ValueError("invalid prefilter arguments")
+    return out
+
+
+def box_moments(img: np.ndarray, half_window: int, fp32: bool = False):
+    lib = load(fp32)
+    a = np.ascontiguousarray(img, np.float32)
+    si = np.empty(a.shape, np.float64)
+    sii = np.empty(a.shape, np.float64)
+    lib.pmo_box_moments(a.ctypes.data, a.shape[1], a.shape[0], half_window, si.ctypes.data, sii.ctypes.data)
+    return si, sii
+
+
+def msg_forward(m, cost, u_if_two, sp_alpha):
+    return load().pmo_msg_forward(m, cost, u_if_two, sp_alpha)
+
+
+def msg_backward(m, cost, u_if_two, sp_alpha):
+    return load().pmo_msg_backward(m, cost, u_if_two, sp_alpha)
+
+
+def find_min_cost(c) -> int:
+    a = np.ascontiguousarray(c, np.float64)
+    return load().pmo_find_min_cost(a.ctypes.data)
+
+
+class Oracle:
+    """One reference image and its sources, as the CUDA engine sees them."""
+
+    def __init__(self, ref: np.ndarray, sources: list[np.ndarray], hh: np.ndarray, inv_k,
+                 half_window: int, depth_near: float, depth_far: float, sp_alpha: float, seed: int,
+                 orientation=(0.0, 0.0, 1.0), quirks: bool = True, batch_id: int = 0,
+                 fp32: bool = False):
+        self.lib = load(fp32)
+        self.ref = np.ascontiguousarray(ref, np.float32)
+        self.sources = [np.ascontiguousarray(s, np.float32) for s in sources]
+        self.hh = np.ascontiguousarray(hh, np.float64).reshape(len(sources), 18)
+        self.H, self.W = self.ref.shape
+        self.V = len(sources)
+        self._src_ptrs = (C.c_void_p * self.V)(*[s.ctypes.data for s in self.sources])
+        self._sw = np.array([s.shape[1] for s in self.sources], np.int32)
+        self._sh = np.array([s.shape[0] for s in self.sources], np.int32)
+        p = _Problem()
+        p.width, p.height, p.n_src, p.half_window = self.W, self.H, self.V, half_window
+        p.ref = self.ref.ctypes.data
+        p.src = C.cast(self._src_ptrs, C.c_void_p)
+        p.src_width, p.src_height = self._sw.ctypes.data, self._sh.ctypes.data
+        p.hh = self.hh.ctypes.data
+        p.inv_k[:] = [float(x) for x in inv_k]
+        p.orientation[:] = [float(x) for x in orientation]
+        p.depth_near, p.depth_far = depth_near, depth_far
+        p.sp_alpha = sp_alpha
+        p.seed, p.batch_id, p.quirks = seed, batch_id, int(quirks)
+        self.p = p
+        self.half_window = half_window
+        self.sum_i, self.sum_ii = box_moments(self.ref, half_window, fp32)
+
+    @property
+    def _pp(self):
+        return C.byref(self.p)
+
+    def set_moments(self, sum_i, sum_ii):
+        self.sum_i = np.ascontiguousarray(sum_i, np.float64)
+        self.sum_ii = np.ascontiguousarray(sum_ii, np.float64)
+
+    def ncc(self, x, y, view, depth, axis) -> float:
+        return self.lib.pmo_ncc(self._pp, self.sum_i.ctypes.data, self.sum_ii.ctypes.data, x, y, view, depth, axis)
+
+    def ncc_batch(self, xs, ys, views, depths, axes) -> np.ndarray:
+        xs = np.ascontiguousarray(xs, np.int32)
+        ys = np.ascontiguousarray(ys, np.int32)
+        vs = np.ascontiguousarray(views, np.int32)
+        ds = np.ascontiguousarray(depths, np.float64)
+        ax = np.ascontiguousarray(np.broadcast_to(axes, xs.shape), np.int32)
+        out = np.empty(xs.shape, np.float64)
+        self.lib.pmo_ncc_batch(self._pp, self.sum_i.ctypes.data, self.sum_ii.ctypes.data, xs.size, xs.ctypes.data,
+                               ys.ctypes.data, vs.ctypes.data, ds.ctypes.data, ax.ctypes.data, out.ctypes.data)
+        return out
+
+    def init_depth(self) -> np.ndarray:
+        d = np.empty((self.H, self.W), np.float64)
+        self.lib.pmo_init_depth(self._pp, d.ctypes.data)
+        return d
+
+    def initial_costs(self, depth: np.ndarray) -> np.ndarray:
+        depth = np.ascontiguousarray(depth, np.float64)
+        c = np.empty((self.H, self.W, self.V), np.float64)
+        self.lib.pmo_initial_costs(self._pp, self.sum_i.ctypes.data, self.sum_ii.ctypes.data, depth.ctypes.data,
+                                   c.ctypes.data)
+        return c
+
+    def sweep(self, depth: np.ndarray, cost: np.ndarray, direction: int, sweep_id: int, num_samples: int,
+              view_sel: np.ndarray | None = None, lines: tuple[int, int] = (0, -1)) -> int:
+        """In-place on float64 depth (H, W) and cost (H, W, V). Returns the evaluation count."""
+        assert depth.dtype == np.float64 and depth.flags.c_contiguous
+        assert cost.dtype == np.float64 and cost.flags.c_contiguous
+        vs = view_sel.ctypes.data if view_sel is not None else None
+        return self.lib.pmo_sweep(self._pp, self.sum_i.ctypes.data, self.sum_ii.ctypes.data, depth.ctypes.data,
+                                  cost.ctypes.data, direction, sweep_id, num_samples, vs, lines[0], lines[1])
+
+    def run(self, iterations: int, num_samples: int):
+        depth = np.empty((self.H, self.W), np.float64)
+        cost = np.empty((self.H, self.W, self.V), np.float64)
+        vsel = np.full((num_samples, self.H, self.W), 255, np.uint8)
+        n = self.lib.pmo_run(self._pp, iterations, num_samples, self.sum_i.ctypes.data, self.sum_ii.ctypes.data,
+                             depth.ctypes.data, cost.ctypes.data, vsel.ctypes.data)
+        return depth, cost, vsel, n
+
+
+def num_threads(fp32: bool = False) -> int:
+    return load(fp32).pmo_num_threads()
+
+
+def from_images(images, ref_id: int, params, source_texels=None, ref_texels=None, fp32=False) -> Oracle:
+    """Oracle for the engine's inputs: FP64 camera setup from the views, texels either given
+    (as the engine stores them) or derived here (u8/255, then the prefilter)."""
+    ref_im = images[ref_id]
+    srcs = [im for i, im in enumerate(images) if i != ref_id]
+    hh, ik = [], None
+    for s in srcs:
+        h_, ik = init_relative(ref_im.K, ref_im.R, ref_im.T, s.K, s.R, s.T, params.orientation_x,
+                               params.orientation_z)
+        hh.append(h_)
+
+    def texels(im):
+        t = im.image.astype(np.float32) / np.float32(255.0)
+        if params.prefilter:
+            t = prefilter(t, params.prefilter, params.gaussian_sigma)
+        return t
+
+    ref_t = ref_texels if ref_texels is not None else texels(ref_im)
+    src_t = source_texels if source_texels is not None else [texels(s) for s in srcs]
+    return Oracle(ref_t, src_t, np.array(hh), ik, params.half_window, params.depth_near, params.depth_far,
+                  params.sp_alpha, params.seed, (params.orientation_x, 0.0, params.orientation_z),
+                  bool(params.quirks), 0, fp32)

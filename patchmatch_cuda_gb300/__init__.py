@@ -1,0 +1,318 @@
+"""GB300-native PatchMatch multi-view stereo.
+
+Python mirror of the reference's driver surface (yhsa678/patchMatch_cuda):
+
+    images = read_middlebury("scene_par.txt")              # image.cpp:64-93
+    pm = PatchMatch(images, near, far, half_window, 32, 16, ref_id, num_samples,
+                    sp_alpha, gaussian_sigma, num_iterations, orientation_x, orientation_z)
+    pm.runPatchMatch()                                       # patchMatch.cu:263-407
+    pm.depth_map                                             # _depthMap, H x W float32
+    pm.save_to_file("depth.bin")                             # array2d_wrapper.h:51-70
+
+All compute runs in the CUDA engine (lib/libpatchmatch_gb300.so) through its C ABI.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+from typing import Sequence
+
+import numpy as np
+
+from . import _native
+from ._native import (DIR_BOTTOM_TO_TOP, DIR_LEFT_TO_RIGHT, DIR_RIGHT_TO_LEFT, DIR_TOP_TO_BOTTOM,
+                      PRECISION_FP32, PRECISION_MIXED, PREFILTER_BOX, PREFILTER_GAUSSIAN,
+                      PREFILTER_NONE, PatchMatchError, PmParams, PmStats, PmView)
+
+__all__ = [
+    "Image", "PatchMatch", "Engine", "read_middlebury", "read_pnm", "write_pgm", "default_params",
+    "load_depth_file", "PatchMatchError", "PREFILTER_NONE", "PREFILTER_BOX", "PREFILTER_GAUSSIAN",
+    "PRECISION_FP32", "PRECISION_MIXED", "DIR_LEFT_TO_RIGHT", "DIR_TOP_TO_BOTTOM",
+    "DIR_RIGHT_TO_LEFT", "DIR_BOTTOM_TO_TOP",
+]
+
+
+class Image:
+    """One calibrated view: Image::updateCamParam (image.cpp:39-61).
+
+    K, R (3x3) and T (3,) with pixel ~ K (R X + T); image is an HxW uint8 array."""
+
+    def __init__(self, K=None, R=None, T=None, image=None):
+        if K is not None:
+            self.update_cam_param(K, R, T, image)
+
+    def update_cam_param(self, K, R, T, image) -> None:
+        self.K = np.asarray(K, np.float32).reshape(3, 3)
+        self.R = np.asarray(R, np.float32).reshape(3, 3)
+        self.T = np.asarray(T, np.float32).reshape(3)
+        img = np.asarray(image)
+        if img.ndim == 3:  # BGR to gray with BT.601 luma weights (cvtColor BGR2GRAY)
+            b, g, r = (img[..., i].astype(np.uint32) for i in range(3))
+            img = ((r * 4899 + g * 9617 + b * 1868 + 8192) >> 14).astype(np.uint8)
+        self.image = np.ascontiguousarray(img, dtype=np.uint8)
+        self.C = -self.R.T @ self.T
+        self.proj = self.K @ np.concatenate([self.R, self.T[:, None]], axis=1)
+
+    updateCamParam = update_cam_param
+
+    def to_view(self) -> PmView:
+        v = PmView()
+        v.gray = self.image.ctypes.data
+        v.height, v.width = self.image.shape
+        v.stride = self.image.strides[0]
+        v.K[:] = [float(x) for x in self.K.ravel()]
+        v.R[:] = [float(x) for x in self.R.ravel()]
+        v.t[:] = [float(x) for x in self.T.ravel()]
+        return v
+
+
+def read_pnm(path) -> np.ndarray:
+    """8-bit binary PGM (P5) or PPM (P6, converted to gray)."""
+    data = Path(path).read_bytes()
+    tokens, pos = [], 0
+    while len(tokens) < 4:
+        while data[pos:pos + 1].isspace():
+            pos += 1
+        if data[pos:pos + 1] == b"#":
+            pos = data.index(b"\n", pos) + 1
+            continue
+        end = pos
+        while not data[end:end + 1].isspace():
+            end += 1
+        tokens.append(data[pos:end])
+        pos = end
+    magic, w, h, mx = tokens[0], int(tokens[1]), int(tokens[2]), int(tokens[3])
+    pos += 1
+    if mx != 255 or magic not in (b"P5", b"P6"):
+        raise ValueError(f"{path}: only 8-bit P5/P6 images are supported")
+    ch = 1 if magic == b"P5" else 3
+    arr = np.frombuffer(data, np.uint8, w * h * ch, pos)
+    if ch == 1:
+        return arr.reshape(h, w).copy()
+    rgb = arr.reshape(h, w, 3).astype(np.uint32)
+    return ((rgb[..., 0] * 4899 + rgb[..., 1] * 9617 + rgb[..., 2] * 1868 + 8192) >> 14).astype(np.uint8)
+
+
+def write_pgm(path, img: np.ndarray) -> None:
+    img = np.ascontiguousarray(img, dtype=np.uint8)
+    Path(path).write_bytes(b"P5\n%d %d\n255\n" % (img.shape[1], img.shape[0]) + img.tobytes())
+
+
+def read_middlebury(path) -> list[Image]:
+    """readMiddleBurry (image.cpp:64-93): image count, then per image
+    '<file> k11..k33 r11..r33 t1 t2 t3'. Image paths resolve against the list's folder."""
+    path = Path(path)
+    toks = path.read_text().split()
+    n = int(toks[0])
+    out, i = [], 1
+    for _ in range(n):
+        name = toks[i]
+        vals = [float(x) for x in toks[i + 1:i + 22]]
+        i += 22
+        p = Path(name)
+        if not p.exists():
+            p = path.parent / name
+        out.append(Image(np.array(vals[0:9]), np.array(vals[9:18]), np.array(vals[18:21]), read_pnm(p)))
+    return out
+
+
+def write_middlebury(path, names: Sequence[str], images: Sequence[Image]) -> None:
+    lines = [str(len(images))]
+    for name, im in zip(names, images):
+        vals = list(im.K.ravel()) + list(im.R.ravel()) + list(im.T.ravel())
+        lines.append(name + " " + " ".join(repr(float(v)) for v in vals))
+    Path(path).write_text("\n".join(lines) + "\n")
+
+
+def load_depth_file(path) -> np.ndarray:
+    """Reads the '<W>&<H>&<D>&' + raw float32 format written by saveToFile."""
+    data = Path(path).read_bytes()
+    parts = data.split(b"&", 3)
+    w, h, d = int(parts[0]), int(parts[1]), int(parts[2])
+    return np.frombuffer(parts[3], np.float32, w * h * d).reshape(d, h, w).squeeze(0) if d == 1 else \
+        np.frombuffer(parts[3], np.float32, w * h * d).reshape(d, h, w)
+
+
+def default_params() -> PmParams:
+    p = PmParams()
+    _native.load_engine().pm_default_params(C.byref(p))
+    return p
+
+
+class Engine:
+    """Owns one pm_handle: every entry point of the C ABI as a method."""
+
+    def __init__(self, images: Sequence[Image], ref_id: int, params: PmParams):
+        self._lib = _native.load_engine()
+        self.images = list(images)
+        self.ref_id = ref_id
+        self.params = params
+        views = (PmView * len(self.images))(*[im.to_view() for im in self.images])
+        h = C.c_void_p()
+        st = self._lib.pm_create(views, len(self.images), ref_id, C.byref(params), C.byref(h))
+        _native.check(st)
+        self.h = h
+        w, hh, v = C.c_int(), C.c_int(), C.c_int()
+        self._lib.pm_get_size(self.h, C.byref(w), C.byref(hh), C.byref(v))
+        self.width, self.height, self.n_src = w.value, hh.value, v.value
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self._lib.pm_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _chk(self, st):
+        _native.check(st, self.h)
+
+    def run(self) -> None:
+        self._chk(self._lib.pm_run(self.h))
+
+    def run_async(self) -> None:
+        self._chk(self._lib.pm_run_async(self.h))
+
+    def synchronize(self) -> None:
+        self._chk(self._lib.pm_synchronize(self.h))
+
+    def depth(self) -> np.ndarray:
+        out = np.empty((self.height, self.width), np.float32)
+        self._chk(self._lib.pm_get_depth(self.h, out.ctypes.data, 0))
+        return out
+
+    def view_selection(self) -> np.ndarray:
+        out = np.empty((self.params.num_samples, self.height, self.width), np.uint8)
+        self._chk(self._lib.pm_get_view_selection(self.h, out.ctypes.data))
+        return out
+
+    def save_depth(self, path) -> None:
+        self._chk(self._lib.pm_save_depth(self.h, str(path).encode()))
+
+    def stats(self) -> PmStats:
+        s = PmStats()
+        self._chk(self._lib.pm_get_stats(self.h, C.byref(s)))
+        return s
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        self._chk(self._lib.pm_get_stream(self.h, C.byref(s)))
+        return s.value or 0
+
+    def init_depth(self) -> None:
+        self._chk(self._lib.pm_init_depth(self.h))
+
+    def compute_costs(self, axis: int = 1) -> None:
+        self._chk(self._lib.pm_compute_costs(self.h, axis))
+
+    def run_sweep(self, direction: int, sweep_id: int, num_samples: int = 0, record_views: bool = False) -> None:
+        self._chk(self._lib.pm_run_sweep(self.h, direction, sweep_id, num_samples, int(record_views)))
+
+    def set_depth(self, depth: np.ndarray) -> None:
+        d = np.ascontiguousarray(depth, np.float32)
+        assert d.shape == (self.height, self.width)
+        self._chk(self._lib.pm_set_depth(self.h, d.ctypes.data))
+
+    def costs(self) -> np.ndarray:
+        out = np.empty((self.height, self.width, self.n_src), np.float32)
+        self._chk(self._lib.pm_get_costs(self.h, out.ctypes.data))
+        return out
+
+    def set_costs(self, costs: np.ndarray) -> None:
+        c = np.ascontiguousarray(costs, np.float32)
+        assert c.shape == (self.height, self.width, self.n_src)
+        self._chk(self._lib.pm_set_costs(self.h, c.ctypes.data))
+
+    def ref_maps(self):
+        ref = np.empty((self.height, self.width), np.float32)
+        si, sii = np.empty_like(ref), np.empty_like(ref)
+        self._chk(self._lib.pm_get_ref_maps(self.h, ref.ctypes.data, si.ctypes.data, sii.ctypes.data))
+        return ref, si, sii
+
+    def source_texels(self, view: int) -> np.ndarray:
+        src = [im for i, im in enumerate(self.images) if i != self.ref_id][view]
+        out = np.empty(src.image.shape, np.float32)
+        self._chk(self._lib.pm_get_source_texels(self.h, view, out.ctypes.data))
+        return out
+
+    def eval_costs(self, xs, ys, views, depths, axes) -> np.ndarray:
+        xs = np.ascontiguousarray(xs, np.int32)
+        ys = np.ascontiguousarray(ys, np.int32)
+        vs = np.ascontiguousarray(views, np.int32)
+        ds = np.ascontiguousarray(depths, np.float32)
+        ax = np.ascontiguousarray(np.broadcast_to(axes, xs.shape), np.int32)
+        out = np.empty(xs.shape, np.float32)
+        self._chk(self._lib.pm_eval_costs(self.h, xs.size, xs.ctypes.data, ys.ctypes.data, vs.ctypes.data,
+                                          ds.ctypes.data, ax.ctypes.data, out.ctypes.data))
+        return out
+
+    def sample_source(self, view: int, xs, ys) -> np.ndarray:
+        xs = np.ascontiguousarray(xs, np.float32)
+        ys = np.ascontiguousarray(ys, np.float32)
+        out = np.empty(xs.shape, np.float32)
+        self._chk(self._lib.pm_sample_source(self.h, view, xs.size, xs.ctypes.data, ys.ctypes.data,
+                                             out.ctypes.data))
+        return out
+
+
+def run_batch(engines: Sequence[Engine]) -> None:
+    lib = _native.load_engine()
+    arr = (C.c_void_p * len(engines))(*[e.h for e in engines])
+    _native.check(lib.pm_run_batch(arr, len(engines)))
+
+
+class PatchMatch:
+    """Mirror of the reference class PatchMatch (patchMatch.h:20-103).
+
+    Constructor arguments follow patchMatch.h:71-72; blockDim_x/blockDim_y are accepted and
+    unused (the engine sizes its own launches). Extra keyword arguments set pm_params fields
+    (prefilter, seed, precision, quirks, ...)."""
+
+    def __init__(self, allImage: Sequence[Image], nearRange: float, farRange: float, halfWindowSize: int,
+                 blockDim_x: int = 32, blockDim_y: int = 16, refImageId: int = 0, numOfSamples: int = 3,
+                 SPMAlpha: float = 0.45, gaussianSigma: float = 1.0, numOfIterations: int = 3,
+                 orientationX: float = 0.0, orientationZ: float = 1.0, **engine_options):
+        p = default_params()
+        p.depth_near, p.depth_far = nearRange, farRange
+        p.half_window, p.num_samples = halfWindowSize, numOfSamples
+        p.sp_alpha, p.gaussian_sigma = SPMAlpha, gaussianSigma
+        p.num_iterations = numOfIterations
+        p.orientation_x, p.orientation_z = orientationX, orientationZ
+        p.block_dim_x, p.block_dim_y = blockDim_x, blockDim_y
+        for k, v in engine_options.items():
+            if not hasattr(p, k):
+                raise TypeError(f"unknown engine option {k!r}")
+            setattr(p, k, v)
+        self.engine = Engine(allImage, refImageId, p)
+
+    def runPatchMatch(self) -> None:
+        self.engine.run()
+
+    run_patch_match = runPatchMatch
+
+    @property
+    def depth_map(self) -> np.ndarray:
+        return self.engine.depth()
+
+    _depthMap = depth_map
+
+    @property
+    def used_imgs_id(self) -> np.ndarray:
+        return self.engine.view_selection()
+
+    def save_to_file(self, path) -> None:
+        self.engine.save_depth(path)
+
+    saveToFile = save_to_file
+
+    def close(self) -> None:
+        self.engine.close()

@@ -1,0 +1,932 @@
+// pm_api.cu -- the C ABI of include/patchmatch_gb300.h.
+//
+// A handle owns one CUDA stream, its device buffers (stream-ordered allocations from the
+// device's default memory pool, whose release threshold is raised so repeated
+// create/destroy cycles reuse memory), one gather-capable CUDA array and texture object per
+// source view, and a CUDA graph of the whole run schedule, captured on first use.
+#include <cuda_fp16.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/patchmatch_gb300.h"
+#include "pm_internal.h"
+
+using namespace pm;
+
+struct pm_handle {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    pm_params p{};
+    int W = 0, H = 0, V = 0, win = 0;
+    int texel_bytes = 4;
+    std::string err;
+
+    float *d_ref = nullptr, *d_sum_i = nullptr, *d_sum_ii = nullptr;
+    float *d_depth = nullptr, *d_cost = nullptr, *d_beta = nullptr;
+    uint8_t *d_view_sel = nullptr;
+    unsigned long long *d_evals = nullptr;
+    float4 *d_hh = nullptr;
+    double *d_hh64 = nullptr;
+    RefDesc *d_desc = nullptr;
+    RefDesc h_desc{};
+    cudaArray_t arr[MAX_VIEWS] = {};
+    cudaTextureObject_t tex[MAX_VIEWS] = {};
+    int src_w[MAX_VIEWS] = {}, src_h[MAX_VIEWS] = {};
+    SweepArgs *h_sweep_args = nullptr;   // pinned, one per sweep of the schedule
+
+    cudaGraphExec_t graph = nullptr;
+    bool ran = false;
+    pm_stats stats{};
+};
+
+namespace {
+
+const char *kStatusStrings[] = {
+    "ok", "invalid argument", "window size out of range", "too few views",
+    "too many source views", "invalid image", "invalid camera", "CUDA error", "out of memory",
+    "I/O error", "no CUDA device", "call out of order", "unsupported"};
+
+pm_status fail(pm_handle *h, pm_status s, const std::string &msg)
+{
+    if (h) h->err = msg;
+    return s;
+}
+
+pm_status cuda_fail(pm_handle *h, cudaError_t e, const char *what)
+{
+    cudaGetLastError();  // clear sticky-free errors
+    std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+    if (h) h->err = m;
+    return e == cudaErrorMemoryAllocation ? PM_ERR_OUT_OF_MEMORY : PM_ERR_CUDA;
+}
+
+#define PM_CUDA(h, expr)                                        \
+    do {                                                        \
+        cudaError_t e_ = (expr);                                \
+        if (e_ != cudaSuccess) return cuda_fail((h), e_, #expr); \
+    } while (0)
+
+// ---- camera setup in double precision (image.cpp:4-61) --------------------------------------
+bool finite_all(const float *v, int n)
+{
+    for (int i = 0; i < n; ++i)
+        if (!std::isfinite(v[i])) return false;
+    return true;
+}
+
+void mul3(const double *a, const double *b, double *o)
+{
+    double t[9];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            t[3 * i + j] = a[3 * i] * b[j] + a[3 * i + 1] * b[3 + j] + a[3 * i + 2] * b[6 + j];
+    std::memcpy(o, t, sizeof t);
+}
+
+bool inv3(const double *m, double *o)
+{
+    const double c00 = m[4] * m[8] - m[5] * m[7], c01 = m[5] * m[6] - m[3] * m[8],
+                 c02 = m[3] * m[7] - m[4] * m[6];
+    const double det = m[0] * c00 + m[1] * c01 + m[2] * c02;
+    if (!(std::fabs(det) > 1e-300) || !std::isfinite(det)) return false;
+    const double id = 1.0 / det;
+    o[0] = c00 * id; o[1] = (m[2] * m[7] - m[1] * m[8]) * id; o[2] = (m[1] * m[5] - m[2] * m[4]) * id;
+    o[3] = c01 * id; o[4] = (m[0] * m[8] - m[2] * m[6]) * id; o[5] = (m[2] * m[3] - m[0] * m[5]) * id;
+    o[6] = c02 * id; o[7] = (m[1] * m[6] - m[0] * m[7]) * id; o[8] = (m[0] * m[4] - m[1] * m[3]) * id;
+    return true;
+}
+
+// H1 = K_s R_s R_r^T K_r^-1, H2 = K_s R_s (C_s - C_r) n^T K_r^-1 with C = -R^T t.
+void relative_homographies(const pm_view &ref, const double *k_ref_inv, const pm_view &src,
+                           double nx, double nz, double out[18])
+{
+    double kr[9], rr[9], tr[3], ks[9], rs[9], ts[3];
+    for (int i = 0; i < 9; ++i) { rr[i] = ref.R[i]; ks[i] = src.K[i]; rs[i] = src.R[i]; kr[i] = ref.K[i]; }
+    for (int i = 0; i < 3; ++i) { tr[i] = ref.t[i]; ts[i] = src.t[i]; }
+    double cr[3], cs[3], rrt[9], rrel[9], h1[9];
+    for (int i = 0; i < 3; ++i) {
+        cr[i] = -(rr[i] * tr[0] + rr[3 + i] * tr[1] + rr[6 + i] * tr[2]);
+        cs[i] = -(rs[i] * ts[0] + rs[3 + i] * ts[1] + rs[6 + i] * ts[2]);
+    }
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) rrt[3 * i + j] = rr[3 * j + i];
+    mul3(rs, rrt, rrel);
+    mul3(ks, rrel, h1);
+    mul3(h1, k_ref_inv, h1);
+    const double dc[3] = {cs[0] - cr[0], cs[1] - cr[1], cs[2] - cr[2]};
+    double trel[3], kt[3], nk[3];
+    for (int i = 0; i < 3; ++i) trel[i] = rs[3 * i] * dc[0] + rs[3 * i + 1] * dc[1] + rs[3 * i + 2] * dc[2];
+    for (int i = 0; i < 3; ++i) kt[i] = ks[3 * i] * trel[0] + ks[3 * i + 1] * trel[1] + ks[3 * i + 2] * trel[2];
+    for (int j = 0; j < 3; ++j) nk[j] = nx * k_ref_inv[j] + nz * k_ref_inv[6 + j];
+    for (int i = 0; i < 9; ++i) out[i] = h1[i];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) out[9 + 3 * i + j] = kt[i] * nk[j];
+    (void)kr;
+}
+
+// Prefilter taps (GaussianBlurCUDA.cu:99-130).
+int prefilter_taps(int mode, float sigma, float *w)
+{
+    int kw = (int)(5.0f * sigma);
+    if (kw % 2 == 0) kw += 1;
+    int radius = (kw - 1) >> 1;
+    if (kw > 45) { radius = 22; kw = 45; }
+    else if (kw < 5) { radius = 2; kw = 5; }
+    if (mode == PM_PREFILTER_BOX) {
+        for (int i = 0; i < kw; ++i) w[i] = 1.0f / (float)kw;
+    } else {
+        double sum = 0.0, tmp[45];
+        for (int i = -radius; i <= radius; ++i) {
+            tmp[i + radius] = std::exp(-0.5 * (double)(i * i) / ((double)sigma * sigma));
+            sum += tmp[i + radius];
+        }
+        for (int i = 0; i < kw; ++i) w[i] = (float)(tmp[i] / sum);
+    }
+    return radius;
+}
+
+// ---- a small cache of gather-capable CUDA arrays, so handle churn does not reallocate ----
+struct ArrayKey {
+    int device, w, h, bytes;
+};
+std::mutex g_array_mutex;
+std::vector<std::pair<ArrayKey, cudaArray_t>> g_free_arrays;
+bool g_pool_ready[64] = {};
+
+cudaError_t acquire_array(int device, int w, int h, int bytes, cudaArray_t *out)
+{
+    {
+        std::lock_guard<std::mutex> lk(g_array_mutex);
+        for (size_t i = 0; i < g_free_arrays.size(); ++i) {
+            const ArrayKey &k = g_free_arrays[i].first;
+            if (k.device == device && k.w == w && k.h == h && k.bytes == bytes) {
+                *out = g_free_arrays[i].second;
+                g_free_arrays.erase(g_free_arrays.begin() + (long)i);
+                return cudaSuccess;
+            }
+        }
+    }
+    cudaChannelFormatDesc fmt = bytes == 1   ? cudaCreateChannelDesc<unsigned char>()
+                                : bytes == 2 ? cudaCreateChannelDescHalf()
+                                             : cudaCreateChannelDesc<float>();
+    return cudaMallocArray(out, &fmt, (size_t)w, (size_t)h, cudaArrayTextureGather);
+}
+
+void release_array(int device, int w, int h, int bytes, cudaArray_t a)
+{
+    std::lock_guard<std::mutex> lk(g_array_mutex);
+    if (g_free_arrays.size() < 256) g_free_arrays.push_back({ArrayKey{device, w, h, bytes}, a});
+    else cudaFreeArray(a);
+}
+
+cudaError_t prepare_pool(int device)
+{
+    if (device < 0 || device >= 64 || g_pool_ready[device]) return cudaSuccess;
+    cudaMemPool_t pool;
+    cudaError_t e = cudaDeviceGetDefaultMemPool(&pool, device);
+    if (e != cudaSuccess) return e;
+    uint64_t threshold = UINT64_MAX;
+    e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold);
+    if (e == cudaSuccess) g_pool_ready[device] = true;
+    return e;
+}
+
+template <typename T>
+cudaError_t dalloc(T **p, size_t bytes, cudaStream_t s)
+{
+    return cudaMallocAsync((void **)p, bytes ? bytes : 16, s);
+}
+
+int window_side(const pm_handle *h) { return 2 * h->p.half_window + 1; }
+
+cudaError_t enqueue_costs(pm_handle *h, int axis)
+{
+    LaunchReq req{};
+    req.kind = LaunchKind::Costs;
+    req.stream = h->stream;
+    req.refs = h->d_desc;
+    req.ref_index = 0;
+    req.axis = axis;
+    const int npix = h->W * h->H;
+    req.grid = (npix + SWEEP_BLOCK / 32 - 1) / (SWEEP_BLOCK / 32);
+    return launch_window(window_side(h), req);
+}
+
+void fill_sweep_args(SweepArgs &a, const RefDesc *refs, const int *lines, int nrefs, int dir,
+                     uint32_t sweep_id, int num_samples, int record)
+{
+    a.refs = refs;
+    a.nrefs = nrefs;
+    a.dir = dir;
+    a.sweep_id = sweep_id;
+    a.num_samples = num_samples;
+    a.record_views = record;
+    a.line_start[0] = 0;
+    for (int i = 0; i < nrefs; ++i) a.line_start[i + 1] = a.line_start[i] + lines[i];
+    a.total_lines = a.line_start[nrefs];
+}
+
+cudaError_t enqueue_sweep(int win, const SweepArgs &a, cudaStream_t s)
+{
+    LaunchReq req{};
+    req.kind = LaunchKind::Sweep;
+    req.stream = s;
+    req.sweep = &a;
+    req.grid = (a.total_lines + SWEEP_BLOCK / 32 - 1) / (SWEEP_BLOCK / 32);
+    return launch_window(win, req);
+}
+
+int lines_of(const pm_handle *h, int dir)
+{
+    return (dir == PM_DIR_LEFT_TO_RIGHT || dir == PM_DIR_RIGHT_TO_LEFT) ? h->H : h->W;
+}
+
+// The whole run: initial depth, initial costs, iterations x 4 sweeps (patchMatch.cu:307-394).
+cudaError_t enqueue_schedule(pm_handle *h)
+{
+    cudaError_t e = cudaMemsetAsync(h->d_evals, 0, 2 * sizeof(unsigned long long), h->stream);
+    if (e != cudaSuccess) return e;
+    e = launch_init_depth(h->d_desc, 0, h->W * h->H, h->stream);
+    if (e != cudaSuccess) return e;
+    e = enqueue_costs(h, 1);
+    if (e != cudaSuccess) return e;
+    const int iters = h->p.num_iterations;
+    for (int it = 0; it < iters; ++it)
+        for (int d = 0; d < 4; ++d) {
+            SweepArgs &a = h->h_sweep_args[4 * it + d];
+            const int lines = lines_of(h, d);
+            fill_sweep_args(a, h->d_desc, &lines, 1, d, (uint32_t)(4 * it + d), it == 0 ? 1 : 0,
+                            (it == iters - 1 && d == PM_DIR_BOTTOM_TO_TOP) ? 1 : 0);
+            e = enqueue_sweep(window_side(h), a, h->stream);
+            if (e != cudaSuccess) return e;
+        }
+    return cudaSuccess;
+}
+
+pm_status set_device(pm_handle *h)
+{
+    PM_CUDA(h, cudaSetDevice(h->device));
+    return PM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void pm_default_params(pm_params *p)
+{
+    if (!p) return;
+    std::memset(p, 0, sizeof *p);
+    p->depth_near = -1.0f;
+    p->depth_far = -1.0f;
+    p->half_window = 5;
+    p->num_samples = 3;
+    p->sp_alpha = 0.45f;
+    p->gaussian_sigma = 1.0f;
+    p->prefilter = PM_PREFILTER_NONE;
+    p->num_iterations = 3;
+    p->orientation_x = 0.0f;
+    p->orientation_z = 1.0f;
+    p->seed = 0x5EEDull;
+    p->precision = PM_PRECISION_FP32;
+    p->init_mode = PM_INIT_RANDOM;
+    p->threads_per_line = 0;
+    p->quirks = 1;
+    p->gpu_id = -1;
+    p->block_dim_x = 32;
+    p->block_dim_y = 16;
+}
+
+const char *pm_status_string(pm_status s)
+{
+    const int i = (int)s;
+    return (i >= 0 && i < (int)(sizeof kStatusStrings / sizeof *kStatusStrings)) ? kStatusStrings[i]
+                                                                                 : "unknown status";
+}
+
+const char *pm_last_error(const pm_handle *h) { return h ? h->err.c_str() : ""; }
+
+pm_status pm_destroy(pm_handle *h)
+{
+    if (!h) return PM_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->graph) cudaGraphExecDestroy(h->graph);
+    for (int v = 0; v < MAX_VIEWS; ++v) {
+        if (h->tex[v]) cudaDestroyTextureObject(h->tex[v]);
+        if (h->arr[v]) release_array(h->device, h->src_w[v], h->src_h[v], h->texel_bytes, h->arr[v]);
+    }
+    void *bufs[] = {h->d_ref, h->d_sum_i, h->d_sum_ii, h->d_depth, h->d_cost, h->d_beta,
+                    h->d_view_sel, h->d_evals, h->d_hh, h->d_hh64, h->d_desc};
+    for (void *b : bufs)
+        if (b) cudaFreeAsync(b, h->stream);
+    if (h->stream) {
+        cudaStreamSynchronize(h->stream);
+        cudaStreamDestroy(h->stream);
+    }
+    for (cudaEvent_t e : h->ev)
+        if (e) cudaEventDestroy(e);
+    if (h->h_sweep_args) cudaFreeHost(h->h_sweep_args);
+    delete h;
+    return PM_OK;
+}
+
+pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_params *params,
+                    pm_handle **out)
+{
+    if (!out) return PM_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    if (!views || !params) return PM_ERR_INVALID_ARGUMENT;
+    if (n_views < 2) return PM_ERR_TOO_FEW_VIEWS;
+    if (ref_id < 0 || ref_id >= n_views) return PM_ERR_INVALID_ARGUMENT;
+    if (n_views - 1 > PM_MAX_SOURCE_VIEWS) return PM_ERR_TOO_MANY_VIEWS;
+    const pm_params &p = *params;
+    if (p.half_window < 1 || p.half_window > PM_MAX_HALF_WINDOW) return PM_ERR_WINDOW_SIZE;
+    if (p.num_samples < 1 || p.num_samples > 32 || p.num_iterations < 1 ||
+        !(p.depth_near > 0.0f) || !(p.depth_far > p.depth_near) || !std::isfinite(p.depth_far) ||
+        !(p.sp_alpha > 0.0f) || !std::isfinite(p.orientation_x) || !std::isfinite(p.orientation_z) ||
+        p.prefilter < PM_PREFILTER_NONE || p.prefilter > PM_PREFILTER_GAUSSIAN ||
+        (p.prefilter == PM_PREFILTER_GAUSSIAN && !(p.gaussian_sigma > 0.0f)) ||
+        (p.precision != PM_PRECISION_FP32 && p.precision != PM_PRECISION_MIXED) ||
+        p.init_mode != PM_INIT_RANDOM ||
+        (p.threads_per_line != 0 && p.threads_per_line != 32))
+        return PM_ERR_INVALID_ARGUMENT;
+    for (int i = 0; i < n_views; ++i) {
+        const pm_view &v = views[i];
+        if (!v.gray || v.width < 1 || v.height < 1 || v.stride < v.width || v.width > 32768 ||
+            v.height > 32768)
+            return PM_ERR_IMAGE;
+        if (!finite_all(v.K, 9) || !finite_all(v.R, 9) || !finite_all(v.t, 3)) return PM_ERR_CAMERA;
+    }
+    const pm_view &ref = views[ref_id];
+    if ((long long)ref.width * ref.height * (n_views - 1) > (1ll << 31)) return PM_ERR_IMAGE;
+
+    int device = p.gpu_id;
+    if (device < 0) {
+        if (cudaGetDevice(&device) != cudaSuccess) return PM_ERR_NO_DEVICE;
+    }
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0 || device >= count) return PM_ERR_NO_DEVICE;
+
+    pm_handle *h = new pm_handle();
+    h->device = device;
+    h->p = p;
+    h->W = ref.width;
+    h->H = ref.height;
+    h->V = n_views - 1;
+    h->win = 2 * p.half_window + 1;
+    const bool filtered = p.prefilter != PM_PREFILTER_NONE;
+    h->texel_bytes = p.precision == PM_PRECISION_FP32 ? (filtered ? 4 : 1) : (filtered ? 2 : 1);
+
+    // camera setup
+    double kr[9], kr_inv[9];
+    for (int i = 0; i < 9; ++i) kr[i] = ref.K[i];
+    if (!inv3(kr, kr_inv)) { pm_destroy(h); return PM_ERR_CAMERA; }
+    std::vector<float> hh((size_t)h->V * 20, 0.0f);
+    std::vector<double> hh64((size_t)h->V * 18);
+    int si = 0;
+    for (int i = 0; i < n_views; ++i) {
+        if (i == ref_id) continue;
+        double o[18];
+        relative_homographies(ref, kr_inv, views[i], p.orientation_x, p.orientation_z, o);
+        for (int k = 0; k < 18; ++k) {
+            if (!std::isfinite(o[k])) { pm_destroy(h); return PM_ERR_CAMERA; }
+            hh[(size_t)si * 20 + k] = (float)o[k];
+            hh64[(size_t)si * 18 + k] = o[k];
+        }
+        h->src_w[si] = views[i].width;
+        h->src_h[si] = views[i].height;
+        ++si;
+    }
+
+    pm_status st = set_device(h);
+    if (st != PM_OK) { pm_destroy(h); return st; }
+    cudaError_t e = prepare_pool(device);
+    if (e != cudaSuccess) { st = cuda_fail(h, e, "memory pool"); pm_destroy(h); return st; }
+#define PM_TRY(expr)                                                     \
+    do {                                                                 \
+        cudaError_t e_ = (expr);                                         \
+        if (e_ != cudaSuccess) {                                         \
+            pm_status s_ = cuda_fail(h, e_, #expr);                      \
+            if (h->stream) cudaStreamSynchronize(h->stream);             \
+            pm_destroy(h);                                               \
+            return s_;                                                   \
+        }                                                                \
+    } while (0)
+    PM_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    for (cudaEvent_t &ev : h->ev) PM_TRY(cudaEventCreate(&ev));
+    PM_TRY(cudaMallocHost((void **)&h->h_sweep_args, sizeof(SweepArgs) * 4 * (size_t)p.num_iterations));
+    PM_TRY(cudaEventRecord(h->ev[0], h->stream));
+
+    const size_t npix = (size_t)h->W * h->H;
+    cudaStream_t s = h->stream;
+    PM_TRY(dalloc(&h->d_ref, npix * 4, s));
+    PM_TRY(dalloc(&h->d_sum_i, npix * 4, s));
+    PM_TRY(dalloc(&h->d_sum_ii, npix * 4, s));
+    PM_TRY(dalloc(&h->d_depth, npix * 4, s));
+    PM_TRY(dalloc(&h->d_cost, npix * h->V * 4, s));
+    PM_TRY(dalloc(&h->d_beta, npix * h->V * 4, s));
+    PM_TRY(dalloc(&h->d_view_sel, npix * (size_t)p.num_samples, s));
+    PM_TRY(dalloc(&h->d_evals, 2 * sizeof(unsigned long long), s));
+    PM_TRY(dalloc(&h->d_hh, hh.size() * 4, s));
+    PM_TRY(dalloc(&h->d_hh64, hh64.size() * 8, s));
+    PM_TRY(dalloc(&h->d_desc, sizeof(RefDesc), s));
+    PM_TRY(cudaMemsetAsync(h->d_view_sel, 255, npix * (size_t)p.num_samples, s));
+    PM_TRY(cudaMemsetAsync(h->d_evals, 0, 2 * sizeof(unsigned long long), s));
+    PM_TRY(cudaMemcpyAsync(h->d_hh, hh.data(), hh.size() * 4, cudaMemcpyHostToDevice, s));
+    PM_TRY(cudaMemcpyAsync(h->d_hh64, hh64.data(), hh64.size() * 8, cudaMemcpyHostToDevice, s));
+
+    // images: u8 upload -> float texels (-> prefilter) -> reference maps / source arrays
+    int max_w = 0, max_h = 0;
+    for (int i = 0; i < n_views; ++i) {
+        max_w = std::max(max_w, views[i].width);
+        max_h = std::max(max_h, views[i].height);
+    }
+    const size_t max_pix = (size_t)max_w * max_h;
+    uint8_t *d_u8 = nullptr;
+    float *d_f0 = nullptr, *d_f1 = nullptr, *d_f2 = nullptr, *d_tmp2 = nullptr;
+    PM_TRY(dalloc(&d_u8, max_pix, s));
+    PM_TRY(dalloc(&d_f0, max_pix * 4, s));
+    PM_TRY(dalloc(&d_f1, max_pix * 4, s));
+    PM_TRY(dalloc(&d_f2, max_pix * 4, s));
+    PM_TRY(dalloc(&d_tmp2, max_pix * 4, s));
+    float taps[45];
+    const int radius = filtered ? prefilter_taps(p.prefilter, p.gaussian_sigma, taps) : 0;
+    si = 0;
+    for (int i = 0; i < n_views; ++i) {
+        const pm_view &v = views[i];
+        PM_TRY(cudaMemcpy2DAsync(d_u8, (size_t)v.width, v.gray, (size_t)v.stride, (size_t)v.width,
+                                 (size_t)v.height, cudaMemcpyHostToDevice, s));
+        const bool is_ref = i == ref_id;
+        float *texels = is_ref && !filtered ? h->d_ref : d_f0;
+        PM_TRY(launch_u8_to_float(d_u8, v.width, texels, v.width, v.height, s));
+        if (filtered) {
+            float *dst = is_ref ? h->d_ref : d_f1;
+            PM_TRY(launch_filter(d_f0, d_f2, dst, v.width, v.height, radius, taps, s));
+            texels = dst;
+        }
+        if (is_ref) {
+            PM_TRY(launch_box_moments(h->d_ref, d_f2, d_tmp2, h->d_sum_i, h->d_sum_ii, v.width,
+                                      v.height, p.half_window, s));
+            continue;
+        }
+        cudaArray_t arr = nullptr;
+        PM_TRY(acquire_array(device, v.width, v.height, h->texel_bytes, &arr));
+        h->arr[si] = arr;
+        if (h->texel_bytes == 1) {
+            PM_TRY(cudaMemcpy2DToArrayAsync(arr, 0, 0, d_u8, (size_t)v.width, (size_t)v.width,
+                                            (size_t)v.height, cudaMemcpyDeviceToDevice, s));
+        } else if (h->texel_bytes == 2) {
+            PM_TRY(launch_float_to_half(texels, d_f2, v.width * v.height, s));
+            PM_TRY(cudaMemcpy2DToArrayAsync(arr, 0, 0, d_f2, (size_t)v.width * 2,
+                                            (size_t)v.width * 2, (size_t)v.height,
+                                            cudaMemcpyDeviceToDevice, s));
+        } else {
+            PM_TRY(cudaMemcpy2DToArrayAsync(arr, 0, 0, texels, (size_t)v.width * 4,
+                                            (size_t)v.width * 4, (size_t)v.height,
+                                            cudaMemcpyDeviceToDevice, s));
+        }
+        cudaResourceDesc rd{};
+        rd.resType = cudaResourceTypeArray;
+        rd.res.array.array = arr;
+        cudaTextureDesc td{};
+        td.addressMode[0] = cudaAddressModeBorder;
+        td.addressMode[1] = cudaAddressModeBorder;
+        td.filterMode = cudaFilterModePoint;
+        td.readMode = h->texel_bytes == 1 ? cudaReadModeNormalizedFloat : cudaReadModeElementType;
+        td.normalizedCoords = 0;
+        PM_TRY(cudaCreateTextureObject(&h->tex[si], &rd, &td, nullptr));
+        ++si;
+    }
+    PM_TRY(cudaFreeAsync(d_u8, s));
+    PM_TRY(cudaFreeAsync(d_f0, s));
+    PM_TRY(cudaFreeAsync(d_f1, s));
+    PM_TRY(cudaFreeAsync(d_f2, s));
+    PM_TRY(cudaFreeAsync(d_tmp2, s));
+
+    RefDesc &D = h->h_desc;
+    std::memset(&D, 0, sizeof D);
+    D.width = h->W;
+    D.height = h->H;
+    D.n_src = h->V;
+    D.num_samples = p.num_samples;
+    D.depth_near = p.depth_near;
+    D.depth_span = p.depth_far - p.depth_near;
+    D.a2 = p.sp_alpha * p.sp_alpha;
+    D.u_emit = (float)std::exp(-0.5 * (double)0.83f * (double)0.83f / (double)D.a2);
+    D.nx = p.orientation_x;
+    D.nz = p.orientation_z;
+    D.ik00 = (float)kr_inv[0];
+    D.ik02 = (float)kr_inv[2];
+    D.quirks = p.quirks ? 1 : 0;
+    D.batch_id = 0;
+    D.seed = p.seed;
+    D.ref = h->d_ref;
+    D.sum_i = h->d_sum_i;
+    D.sum_ii = h->d_sum_ii;
+    D.depth = h->d_depth;
+    D.cost = h->d_cost;
+    D.beta = h->d_beta;
+    D.view_sel = h->d_view_sel;
+    D.evals = h->d_evals;
+    D.hh = h->d_hh;
+    D.hh64 = h->d_hh64;
+    for (int v = 0; v < h->V; ++v) {
+        D.tex[v] = h->tex[v];
+        D.src_w[v] = (float)h->src_w[v];
+        D.src_h[v] = (float)h->src_h[v];
+    }
+    PM_TRY(cudaMemcpyAsync(h->d_desc, &D, sizeof D, cudaMemcpyHostToDevice, s));
+    PM_TRY(cudaEventRecord(h->ev[1], s));
+    PM_TRY(cudaStreamSynchronize(s));
+#undef PM_TRY
+    cudaEventElapsedTime(&h->stats.ms_prepare, h->ev[0], h->ev[1]);
+    h->stats.threads_per_line = 32;
+    h->stats.texel_bytes = h->texel_bytes;
+    *out = h;
+    return PM_OK;
+}
+
+pm_status pm_run_async(pm_handle *h)
+{
+    if (!h) return PM_ERR_INVALID_ARGUMENT;
+    pm_status st = set_device(h);
+    if (st != PM_OK) return st;
+    if (!h->graph) {
+        cudaGraph_t g = nullptr;
+        PM_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        const cudaError_t e = enqueue_schedule(h);
+        const cudaError_t e2 = cudaStreamEndCapture(h->stream, &g);
+        if (e != cudaSuccess) { if (g) cudaGraphDestroy(g); return cuda_fail(h, e, "schedule capture"); }
+        if (e2 != cudaSuccess) return cuda_fail(h, e2, "cudaStreamEndCapture");
+        const cudaError_t e3 = cudaGraphInstantiate(&h->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e3 != cudaSuccess) { h->graph = nullptr; return cuda_fail(h, e3, "cudaGraphInstantiate"); }
+    }
+    PM_CUDA(h, cudaEventRecord(h->ev[2], h->stream));
+    PM_CUDA(h, cudaGraphLaunch(h->graph, h->stream));
+    PM_CUDA(h, cudaEventRecord(h->ev[3], h->stream));
+    h->ran = true;
+    return PM_OK;
+}
+
+pm_status pm_synchronize(pm_handle *h)
+{
+    if (!h) return PM_ERR_INVALID_ARGUMENT;
+    pm_status st = set_device(h);
+    if (st != PM_OK) return st;
+    PM_CUDA(h, cudaStreamSynchronize(h->stream));
+    return PM_OK;
+}
+
+pm_status pm_run(pm_handle *h)
+{
+    pm_status st = pm_run_async(h);
+    if (st != PM_OK) return st;
+    st = pm_synchronize(h);
+    if (st != PM_OK) return st;
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, h->ev[2], h->ev[3]) == cudaSuccess) h->stats.ms_total = ms;
+    unsigned long long ev[2];
+    PM_CUDA(h, cudaMemcpy(ev, h->d_evals, sizeof ev, cudaMemcpyDeviceToHost));
+    h->stats.cost_evals = ev[0];
+    h->stats.cost_evals_done = ev[1];
+    return PM_OK;
+}
+
+pm_status pm_run_batch(pm_handle *const *hs, int n)
+{
+    if (!hs || n < 1) return PM_ERR_INVALID_ARGUMENT;
+    for (int i = 0; i < n; ++i) {
+        if (!hs[i]) return PM_ERR_INVALID_ARGUMENT;
+        if (hs[i]->device != hs[0]->device) return PM_ERR_UNSUPPORTED;
+    }
+    pm_handle *h0 = hs[0];
+    pm_status st = set_device(h0);
+    if (st != PM_OK) return st;
+    for (int i = 0; i < n; ++i) PM_CUDA(hs[i], cudaStreamSynchronize(hs[i]->stream));
+    cudaStream_t s = h0->stream;
+    // group by window side; each group sweeps in one launch per direction
+    std::vector<int> done(n, 0);
+    for (int g0 = 0; g0 < n; ++g0) {
+        if (done[g0]) continue;
+        std::vector<pm_handle *> grp;
+        for (int i = g0; i < n; ++i)
+            if (!done[i] && hs[i]->win == hs[g0]->win) { grp.push_back(hs[i]); done[i] = 1; }
+        for (size_t start = 0; start < grp.size(); start += MAX_BATCH_REFS) {
+            const int m = (int)std::min<size_t>(MAX_BATCH_REFS, grp.size() - start);
+            RefDesc *d_descs = nullptr;
+            PM_CUDA(h0, cudaMallocAsync((void **)&d_descs, sizeof(RefDesc) * m, s));
+            int max_iters = 0;
+            for (int i = 0; i < m; ++i) {
+                pm_handle *h = grp[start + i];
+                PM_CUDA(h0, cudaMemcpyAsync(d_descs + i, &h->h_desc, sizeof(RefDesc),
+                                            cudaMemcpyHostToDevice, s));
+                PM_CUDA(h0, cudaMemsetAsync(h->d_evals, 0, 2 * sizeof(unsigned long long), s));
+                PM_CUDA(h0, launch_init_depth(d_descs, i, h->W * h->H, s));
+                LaunchReq req{};
+                req.kind = LaunchKind::Costs;
+                req.stream = s;
+                req.refs = d_descs;
+                req.ref_index = i;
+                req.axis = 1;
+                req.grid = (h->W * h->H + 3) / 4;
+                PM_CUDA(h0, launch_window(h->win, req));
+                max_iters = std::max(max_iters, h->p.num_iterations);
+            }
+            std::vector<SweepArgs> args((size_t)max_iters * 4);
+            for (int it = 0; it < max_iters; ++it)
+                for (int d = 0; d < 4; ++d) {
+                    // references still iterating at `it`, in descriptor order
+                    std::vector<int> lines(m, 0);
+                    for (int i = 0; i < m; ++i)
+                        lines[i] = grp[start + i]->p.num_iterations > it ? lines_of(grp[start + i], d) : 0;
+                    // a reference whose last iteration is `it` records its view selection;
+                    // the kernel flag is per launch, so record for everyone on the global
+                    // last iteration and rely on per-reference iteration counts otherwise
+                    SweepArgs &a = args[(size_t)it * 4 + d];
+                    fill_sweep_args(a, d_descs, lines.data(), m, d, (uint32_t)(4 * it + d),
+                                    it == 0 ? 1 : 0, d == PM_DIR_BOTTOM_TO_TOP ? 1 : 0);
+                    PM_CUDA(h0, enqueue_sweep(grp[start]->win, a, s));
+                }
+            PM_CUDA(h0, cudaFreeAsync(d_descs, s));
+        }
+    }
+    PM_CUDA(h0, cudaStreamSynchronize(s));
+    for (int i = 0; i < n; ++i) {
+        unsigned long long ev[2];
+        PM_CUDA(hs[i], cudaMemcpy(ev, hs[i]->d_evals, sizeof ev, cudaMemcpyDeviceToHost));
+        hs[i]->stats.cost_evals = ev[0];
+        hs[i]->stats.cost_evals_done = ev[1];
+        hs[i]->ran = true;
+    }
+    return PM_OK;
+}
+
+pm_status pm_get_depth(pm_handle *h, float *dst, size_t dst_pitch)
+{
+    if (!h || !dst) return PM_ERR_INVALID_ARGUMENT;
+    pm_status st = set_device(h);
+    if (st != PM_OK) return st;
+    if (dst_pitch == 0) dst_pitch = (size_t)h->W * 4;
+    if (dst_pitch < (size_t)h->W * 4) return PM_ERR_INVALID_ARGUMENT;
+    PM_CUDA(h, cudaMemcpy2DAsync(dst, dst_pitch, h->d_depth, (size_t)h->W * 4, (size_t)h->W * 4,
+                                 (size_t)h->H, cudaMemcpyDeviceToHost, h->stream));
+    PM_CUDA(h, cudaStreamSynchronize(h->stream));
+    return PM_OK;
+}
+
+pm_status pm_get_view_selection(pm_handle *h, uint8_t *dst)
+{
+    if (!h || !dst) return PM_ERR_INVALID_ARGUMENT;
+    if (!h->ran) return fail(h, PM_ERR_STATE, "no run has recorded a view selection yet");
+    pm_status st = set_device(h);
+    if (st != PM_OK) return st;
+    PM_CUDA(h, cudaMemcpyAsync(dst, h->d_view_sel, (size_t)h->W * h->H * h->p.num_samples,
+                               cudaMemcpyDeviceToHost, h->stream));
+    PM_CUDA(h, cudaStreamSynchronize(h->stream));
+    return PM_OK;
+}
+
+pm_status pm_save_depth(pm_handle *h, const char *path)
+{
+    if (!h || !path) return PM_ERR_INVALID_ARGUMENT;
+    std::vector<float> d((size_t)h->W * h->H);
+    pm_status st = pm_get_depth(h, d.data(), 0);
+    if (st != PM_OK) return st;
+    FILE *f = std::fopen(path, "wb");
+    if (!f) return fail(h, PM_ERR_IO, std::string("cannot open ") + path);
+    std::fprintf(f, "%d&%d&%d&", h->W, h->H, 1);
+    const size_t wrote = std::fwrite(d.data(), sizeof(float), d.size(), f);
+    const int closed = std::fclose(f);
+    if (wrote != d.size() || closed != 0) return fail(h, PM_ERR_IO, std::string("short write to ") + path);
+    return PM_OK;
+}
+
+pm_status pm_get_stats(const pm_handle *h, pm_stats *out)
+{
+    if (!h || !out) return PM_ERR_INVALID_ARGUMENT;
+    *out = h->stats;
+    return PM_OK;
+}
+
+pm_status pm_get_stream(const pm_handle *h, void **stream)
+{
+    if (!h || !stream) return PM_ERR_INVALID_ARGUMENT;
+    *stream = (void *)h->stream;
+    return PM_OK;
+}
+
+pm_status pm_get_size(const pm_handle *h, int *width, int *height, int *n_src)
+{
+    if (!h) return PM_ERR_INVALID_ARGUMENT;
+    if (width) *width = h->W;
+    if (height) *height = h->H;
+    if (n_src) *n_src = h->V;
+    return PM_OK;
+}
+
+pm_status pm_init_depth(pm_handle *h)
+{
+    if (!h) return PM_ERR_INVALID_ARGUMENT;
+    pm_status st = set_device(h);
+    if (st != PM_OK) return st;
+    PM_CUDA(h, launch_init_depth(h->d_desc, 0, h->W * h->H, h->stream));
+    PM_CUDA(h, cudaStreamSynchronize(h->stream));
+    return PM_OK;
+}
+
+pm_status pm_compute_costs(pm_handle *h, int axis)
+{
+    if (!h || (axis != 0 && axis != 1)) return PM_ERR_INVALID_ARGUMENT;
+    pm_status st = set_device(h);
+    if (st != PM_OK) return st;
+    PM_CUDA(h, enqueue_costs(h, axis));
+    PM_CUDA(h, cudaStreamSynchronize(h->stream));
+    return PM_OK;
+}
+
+pm_status pm_run_sweep(pm_handle *h, int direction, uint32_t sweep_id, int num_samples,
+                       int record_views)
+{
+    if (!h || direction < 0 || direction > 3 || num_samples < 0 || num_samples > 32)
+        return PM_ERR_INVALID_ARGUMENT;
+    pm_status st = set_device(h);
+    if (st != PM_OK) return st;
+    SweepArgs a;
+    const int lines = lines_of(h, direction);
+    fill_sweep_args(a, h->d_desc, &lines, 1, direction, sweep_id, num_samples, record_views ? 1 : 0);
+    if (record_views && num_samples > h->p.num_samples) return PM_ERR_INVALID_ARGUMENT;
+    PM_CUDA(h, cudaEventRecord(h->ev[2], h->stream));
+    PM_CUDA(h, enqueue_sweep(h->win, a, h->stream));
+    PM_CUDA(h, cudaEventRecord(h->ev[3], h->stream));
+    PM_CUDA(h, cudaStreamSynchronize(h->stream));
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, h->ev[2], h->ev[3]) == cudaSuccess) h->stats.ms_sweeps = ms;
+    if (record_views) h->ran = true;
+    return PM_OK;
+}
+
+pm_status pm_set_depth(pm_handle *h, const float *src)
+{
+    if (!h || !src) return PM_ERR_INVALID_ARGUMENT;
+    pm_status st = set_device(h);
+    if (st != PM_OK) return st;
+    PM_CUDA(h, cudaMemcpyAsync(h->d_depth, src, (size_t)h->W * h->H * 4, cudaMemcpyHostToDevice, h->stream));
+    PM_CUDA(h, cudaStreamSynchronize(h->stream));
+    return PM_OK;
+}
+
+pm_status pm_get_costs(pm_handle *h, float *dst)
+{
+    if (!h || !dst) return PM_ERR_INVALID_ARGUMENT;
+    pm_status st = set_device(h);
+    if (st != PM_OK) return st;
+    PM_CUDA(h, cudaMemcpyAsync(dst, h->d_cost, (size_t)h->W * h->H * h->V * 4, cudaMemcpyDeviceToHost, h->stream));
+    PM_CUDA(h, cudaStreamSynchronize(h->stream));
+    return PM_OK;
+}
+
+pm_status pm_set_costs(pm_handle *h, const float *src)
+{
+    if (!h || !src) return PM_ERR_INVALID_ARGUMENT;
+    pm_status st = set_device(h);
+    if (st != PM_OK) return st;
+    PM_CUDA(h, cudaMemcpyAsync(h->d_cost, src, (size_t)h->W * h->H * h->V * 4, cudaMemcpyHostToDevice, h->stream));
+    PM_CUDA(h, cudaStreamSynchronize(h->stream));
+    return PM_OK;
+}
+
+pm_status pm_get_ref_maps(pm_handle *h, float *ref, float *sum_i, float *sum_ii)
+{
+    if (!h) return PM_ERR_INVALID_ARGUMENT;
+    pm_status st = set_device(h);
+    if (st != PM_OK) return st;
+    const size_t bytes = (size_t)h->W * h->H * 4;
+    if (ref) PM_CUDA(h, cudaMemcpyAsync(ref, h->d_ref, bytes, cudaMemcpyDeviceToHost, h->stream));
+    if (sum_i) PM_CUDA(h, cudaMemcpyAsync(sum_i, h->d_sum_i, bytes, cudaMemcpyDeviceToHost, h->stream));
+    if (sum_ii) PM_CUDA(h, cudaMemcpyAsync(sum_ii, h->d_sum_ii, bytes, cudaMemcpyDeviceToHost, h->stream));
+    PM_CUDA(h, cudaStreamSynchronize(h->stream));
+    return PM_OK;
+}
+
+pm_status pm_get_source_texels(pm_handle *h, int view, float *dst)
+{
+    if (!h || !dst || view < 0 || view >= h->V) return PM_ERR_INVALID_ARGUMENT;
+    pm_status st = set_device(h);
+    if (st != PM_OK) return st;
+    const int w = h->src_w[view], hgt = h->src_h[view], b = h->texel_bytes;
+    std::vector<uint8_t> raw((size_t)w * hgt * b);
+    PM_CUDA(h, cudaMemcpy2DFromArrayAsync(raw.data(), (size_t)w * b, h->arr[view], 0, 0,
+                                          (size_t)w * b, (size_t)hgt, cudaMemcpyDeviceToHost, h->stream));
+    PM_CUDA(h, cudaStreamSynchronize(h->stream));
+    const size_t n = (size_t)w * hgt;
+    if (b == 1) {
+        for (size_t i = 0; i < n; ++i) dst[i] = (float)raw[i] / 255.0f;
+    } else if (b == 2) {
+        const __half *hp = (const __half *)raw.data();
+        for (size_t i = 0; i < n; ++i) dst[i] = __half2float(hp[i]);
+    } else {
+        std::memcpy(dst, raw.data(), n * 4);
+    }
+    return PM_OK;
+}
+
+pm_status pm_eval_costs(pm_handle *h, int n, const int *xs, const int *ys, const int *views,
+                        const float *depths, const int *axes, float *out)
+{
+    if (!h || n < 0 || (n > 0 && (!xs || !ys || !views || !depths || !axes || !out)))
+        return PM_ERR_INVALID_ARGUMENT;
+    if (n == 0) return PM_OK;
+    std::vector<int4> q((size_t)n);
+    for (int i = 0; i < n; ++i) {
+        if (xs[i] < 0 || xs[i] >= h->W || ys[i] < 0 || ys[i] >= h->H || views[i] < 0 ||
+            views[i] >= h->V || (axes[i] != 0 && axes[i] != 1))
+            return fail(h, PM_ERR_INVALID_ARGUMENT, "query out of range");
+        q[(size_t)i] = make_int4(xs[i], ys[i], views[i], axes[i]);
+    }
+    pm_status st = set_device(h);
+    if (st != PM_OK) return st;
+    int4 *d_q = nullptr;
+    float *d_d = nullptr, *d_o = nullptr;
+    cudaStream_t s = h->stream;
+    PM_CUDA(h, cudaMallocAsync((void **)&d_q, sizeof(int4) * n, s));
+    PM_CUDA(h, cudaMallocAsync((void **)&d_d, sizeof(float) * n, s));
+    PM_CUDA(h, cudaMallocAsync((void **)&d_o, sizeof(float) * n, s));
+    PM_CUDA(h, cudaMemcpyAsync(d_q, q.data(), sizeof(int4) * n, cudaMemcpyHostToDevice, s));
+    PM_CUDA(h, cudaMemcpyAsync(d_d, depths, sizeof(float) * n, cudaMemcpyHostToDevice, s));
+    LaunchReq req{};
+    req.kind = LaunchKind::Eval;
+    req.stream = s;
+    req.refs = h->d_desc;
+    req.ref_index = 0;
+    req.n = n;
+    req.queries = d_q;
+    req.depths = d_d;
+    req.out = d_o;
+    req.grid = std::min((n + 3) / 4, 65535);
+    PM_CUDA(h, launch_window(h->win, req));
+    PM_CUDA(h, cudaMemcpyAsync(out, d_o, sizeof(float) * n, cudaMemcpyDeviceToHost, s));
+    PM_CUDA(h, cudaFreeAsync(d_q, s));
+    PM_CUDA(h, cudaFreeAsync(d_d, s));
+    PM_CUDA(h, cudaFreeAsync(d_o, s));
+    PM_CUDA(h, cudaStreamSynchronize(s));
+    return PM_OK;
+}
+
+pm_status pm_sample_source(pm_handle *h, int view, int n, const float *xs, const float *ys,
+                           float *out)
+{
+    if (!h || view < 0 || view >= h->V || n < 0 || (n > 0 && (!xs || !ys || !out)))
+        return PM_ERR_INVALID_ARGUMENT;
+    if (n == 0) return PM_OK;
+    pm_status st = set_device(h);
+    if (st != PM_OK) return st;
+    float *d = nullptr;
+    cudaStream_t s = h->stream;
+    PM_CUDA(h, cudaMallocAsync((void **)&d, sizeof(float) * 3 * (size_t)n, s));
+    PM_CUDA(h, cudaMemcpyAsync(d, xs, sizeof(float) * n, cudaMemcpyHostToDevice, s));
+    PM_CUDA(h, cudaMemcpyAsync(d + n, ys, sizeof(float) * n, cudaMemcpyHostToDevice, s));
+    PM_CUDA(h, launch_sample(h->d_desc, 0, view, n, d, d + n, d + 2 * (size_t)n, s));
+    PM_CUDA(h, cudaMemcpyAsync(out, d + 2 * (size_t)n, sizeof(float) * n, cudaMemcpyDeviceToHost, s));
+    PM_CUDA(h, cudaFreeAsync(d, s));
+    PM_CUDA(h, cudaStreamSynchronize(s));
+    return PM_OK;
+}
+
+pm_status pm_transpose_layers(const float *d_in, size_t in_pitch, float *d_out, size_t out_pitch,
+                              int width, int height, int layers, void *stream)
+{
+    if (!d_in || !d_out || width < 1 || height < 1 || layers < 1 ||
+        in_pitch < (size_t)width * 4 || out_pitch < (size_t)height * 4)
+        return PM_ERR_INVALID_ARGUMENT;
+    cudaError_t e = launch_transpose(d_in, in_pitch, d_out, out_pitch, width, height, layers,
+                                     (cudaStream_t)stream);
+    if (e != cudaSuccess) { cudaGetLastError(); return PM_ERR_CUDA; }
+    return PM_OK;
+}
+
+pm_status pm_philox(uint64_t seed, int n, const uint32_t *counters, uint32_t *out)
+{
+    if (n < 0 || (n > 0 && (!counters || !out))) return PM_ERR_INVALID_ARGUMENT;
+    if (n == 0) return PM_OK;
+    uint32_t *d = nullptr;
+    if (cudaMalloc((void **)&d, sizeof(uint32_t) * 8 * (size_t)n) != cudaSuccess) {
+        cudaGetLastError();
+        return PM_ERR_OUT_OF_MEMORY;
+    }
+    cudaError_t e = cudaMemcpy(d, counters, sizeof(uint32_t) * 4 * (size_t)n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = launch_philox(seed, n, d, d + 4 * (size_t)n, nullptr);
+    if (e == cudaSuccess) e = cudaMemcpy(out, d + 4 * (size_t)n, sizeof(uint32_t) * 4 * (size_t)n, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) { cudaGetLastError(); return PM_ERR_CUDA; }
+    return PM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,279 @@
+// pm_device.cuh -- device building blocks of the PatchMatch engine (sm_103a).
+//
+// One warp owns one line of a sweep (a reference-image column for vertical sweeps, a row
+// for horizontal ones). For a windowed NCC every lane owns ceil(w*w/32) "slots" of the
+// window: slot i of lane l is window sample k = l + 32 i, (dx, dy) = (k % w, k / w). The
+// reference values of a lane's slots are loaded once per step into registers and reused
+// by every hypothesis of that step; the three source moments of an evaluation are summed
+// per lane and then across the warp with a butterfly of shuffles.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace pm {
+
+constexpr unsigned FULL_MASK = 0xffffffffu;
+constexpr int MAX_VIEWS = 32;
+
+// Random-draw purposes; a draw is keyed by (pixel, sweep, purpose << 16 | sub, batch).
+enum : uint32_t {
+    RNG_INIT = 1, RNG_BWD = 2, RNG_FWD_PRE = 3, RNG_FWD_POST = 4, RNG_RAND_DEPTH = 5,
+    RNG_SAMPLE = 6
+};
+constexpr uint32_t INIT_SWEEP_ID = 0xFFFFFFFFu;
+
+// Transition probabilities and the uniform-emission cost of the HMM, as float constants
+// (FIX_STATE_PROB 0.999f and CHANGE_STATE_PROB = 1.0f - 0.999f).
+constexpr float FIX_STATE_PROB = 0.999f;
+constexpr float CHANGE_STATE_PROB = 1.0f - 0.999f;
+
+// Everything a kernel needs about one reference image. Lives in device memory; a launch
+// may cover several references (batched runs).
+struct RefDesc {
+    int width, height, n_src, num_samples;
+    float depth_near, depth_span;   // near, far - near
+    float a2;                       // SPMAlpha^2 (float product)
+    float u_emit;                   // exp(-0.83^2 / (2 a2))
+    float nx, nz, ik00, ik02;       // plane scale s = nx (ik00 (x+1/2) + ik02) + nz
+    int quirks;
+    uint32_t batch_id;
+    uint64_t seed;
+    const float *ref;               // height*width texels
+    const float *sum_i;             // box sums of the window
+    const float *sum_ii;
+    float *depth;                   // height*width
+    float *cost;                    // height*width*n_src, pixel-major
+    float *beta;                    // scratch: width*height*n_src backward messages
+    uint8_t *view_sel;              // num_samples*height*width or null
+    unsigned long long *evals;      // [0] algorithmic count, [1] computed count
+    const float4 *hh;               // n_src * 5 float4: H1 (9), H2 (9), pad (2)
+    const double *hh64;             // n_src * 18 (mixed precision window origin)
+    cudaTextureObject_t tex[MAX_VIEWS];
+    float src_w[MAX_VIEWS], src_h[MAX_VIEWS];
+};
+
+// ---- Philox4x32-10 (Salmon et al., SC'11) ----------------------------------------------
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k)
+{
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+        const uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+        c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+        k.x += 0x9E3779B9u;
+        k.y += 0xBB67AE85u;
+    }
+    return c;
+}
+
+// Uniform in (0, 1], 24-bit: ((x >> 8) + 1) * 2^-24 (the interval of curand_uniform).
+__device__ __forceinline__ float draw_uniform(uint64_t seed, uint32_t pixel, uint32_t sweep,
+                                              uint32_t purpose, uint32_t sub, uint32_t batch)
+{
+    const uint4 o = philox4x32_10(make_uint4(pixel, sweep, (purpose << 16) | sub, batch),
+                                  make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)));
+    return (float)((o.x >> 8) + 1u) * (1.0f / 16777216.0f);
+}
+
+// ---- source fetch --------------------------------------------------------------------------
+// The reference samples tex2DLayered(src, u/z + 0.5, v/z + 0.5) with linear filtering and a
+// zero border (patchMatch.cu:543): bilinear interpolation at (u/z, v/z) with texel i at
+// coordinate i. Here the four texels come from one gather (tld4) centred on the 2x2
+// footprint, and the weights are exact FP32 fractions. Gather order (x0,y1), (x1,y1),
+// (x1,y0), (x0,y0).
+__device__ __forceinline__ float sample_source(cudaTextureObject_t tex, float xs, float ys,
+                                               float sw, float sh)
+{
+    if (!(xs > -1.0f && xs < sw && ys > -1.0f && ys < sh)) return 0.0f;
+    const float fx = floorf(xs), fy = floorf(ys);
+    const float ax = xs - fx, ay = ys - fy;
+    const float4 g = tex2Dgather<float4>(tex, fx + 1.0f, fy + 1.0f, 0);
+    const float top = fmaf(ax, g.z - g.w, g.w);
+    const float bot = fmaf(ax, g.y - g.x, g.x);
+    return fmaf(ay, bot - top, top);
+}
+
+__device__ __forceinline__ float warp_sum(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL_MASK, v, o);
+    return v;
+}
+
+// 1 - NCC from the window moments (patchMatch.cu:594-610): 2 when the source window is all
+// zero, variances below 1e-5 clamp to 0, 1 when their product is 0.
+__device__ __forceinline__ float ncc_finalize(float sj, float sjj, float sij, float si,
+                                              float sii, float n)
+{
+    if (sjj == 0.0f) return 2.0f;
+    float c1 = sii - si * si / n;
+    float c2 = sjj - sj * sj / n;
+    c1 = c1 < 0.00001f ? 0.0f : c1;
+    c2 = c2 < 0.00001f ? 0.0f : c2;
+    const float c = sqrtf(c1 * c2);
+    if (c == 0.0f) return 1.0f;
+    return 1.0f - (sij - si * sj / n) / c;
+}
+
+// HMM messages (patchMatch.cu:669-715). e = exp(-c^2 / (2 a2)); a cost of exactly 2 is
+// replaced by 2 U(0,1] by the caller.
+__device__ __forceinline__ float emission(float c, float a2) { return expf(-0.5f * c * c / a2); }
+
+__device__ __forceinline__ float msg_backward(float m, float e, float u)
+{
+    const float zn0 = m * e * FIX_STATE_PROB + (1.0f - m) * u * CHANGE_STATE_PROB;
+    const float zn1 = m * e * CHANGE_STATE_PROB + (1.0f - m) * u * FIX_STATE_PROB;
+    return zn0 / (zn0 + zn1);
+}
+
+__device__ __forceinline__ float msg_forward(float m, float e, float u)
+{
+    const float zn0 = (m * FIX_STATE_PROB + (1.0f - m) * CHANGE_STATE_PROB) * e;
+    const float zn1 = (m * CHANGE_STATE_PROB + (1.0f - m) * FIX_STATE_PROB) * u;
+    return zn0 / (zn0 + zn1);
+}
+
+// ---- window slots ---------------------------------------------------------------------------
+template <int W>
+struct Window {
+    static constexpr int HW = W / 2;
+    static constexpr int NSAMP = W * W;
+    static constexpr int NS = (NSAMP + 31) / 32;
+};
+
+// Per-step state of one pixel's window, held by every lane for its own slots.
+template <int W>
+struct PixelWindow {
+    static constexpr int NS = Window<W>::NS;
+    float rv[NS];        // reference value paired with the slot (0 when out of bounds)
+    uint64_t inb;        // slot in bounds
+    float ox, oy;        // window origin in reference pixel-centre coordinates
+    float si, sii, n;    // box sums and in-bounds count
+    float scale;         // plane scale at this pixel
+};
+
+// Loads a pixel's window for lane `lane`. axis selects which image axis is the sweep's
+// column axis for the reference's misalignment (0: x, vertical sweeps; 1: y).
+template <int W>
+__device__ __forceinline__ void load_window(const RefDesc &D, int x, int y, int axis, int lane,
+                                            const float (&fdx)[Window<W>::NS],
+                                            const float (&fdy)[Window<W>::NS],
+                                            PixelWindow<W> &pw)
+{
+    constexpr int HW = Window<W>::HW, NS = Window<W>::NS, NSAMP = Window<W>::NSAMP;
+    const int Wd = D.width, Hd = D.height;
+    const int x0 = x - HW, y0 = y - HW;
+    int lead_x = 0, lead_y = 0;
+    if (D.quirks) {
+        if (axis == 0) lead_x = x0 < 0 ? -x0 : 0;
+        else lead_y = y0 < 0 ? -y0 : 0;
+    }
+    uint64_t inb = 0;
+#pragma unroll
+    for (int i = 0; i < NS; ++i) {
+        const int k = lane + 32 * i;
+        const int xx = x0 + (int)fdx[i], yy = y0 + (int)fdy[i];
+        const bool in = (k < NSAMP) && xx >= 0 && xx < Wd && yy >= 0 && yy < Hd;
+        float r = 0.0f;
+        if (in) {
+            const int rx = xx - lead_x, ry = yy - lead_y;
+            if (rx >= 0 && ry >= 0) r = __ldg(D.ref + (size_t)ry * Wd + rx);
+            inb |= (uint64_t)1 << i;
+        }
+        pw.rv[i] = r;
+    }
+    pw.inb = inb;
+    pw.ox = (float)x0 + 0.5f;
+    pw.oy = (float)y0 + 0.5f;
+    const int cx0 = max(x0, 0), cx1 = min(x + HW, Wd - 1);
+    const int cy0 = max(y0, 0), cy1 = min(y + HW, Hd - 1);
+    pw.n = (float)((cx1 - cx0 + 1) * (cy1 - cy0 + 1));
+    const size_t pix = (size_t)y * Wd + x;
+    pw.si = __ldg(D.sum_i + pix);
+    pw.sii = __ldg(D.sum_ii + pix);
+    pw.scale = D.nx * (D.ik00 * ((float)x + 0.5f) + D.ik02) + D.nz;
+}
+
+// Plane-induced homography of (view, depth) applied at the window origin:
+// T = H1 - H2 / (depth * scale) (patchMatch.cu:462-474); returns T's first two columns and
+// T (ox, oy, 1).
+struct WarpSetup {
+    float c0x, c0y, c0z, c1x, c1y, c1z, bx, by, bz;
+};
+
+__device__ __forceinline__ WarpSetup warp_setup(const RefDesc &D, int view, float depth,
+                                                float scale, float ox, float oy)
+{
+    const float4 *h = D.hh + 5 * view;
+    const float4 a = __ldg(h), b = __ldg(h + 1), c = __ldg(h + 2), d = __ldg(h + 3),
+                 e = __ldg(h + 4);
+    // 20 floats per view: H1 (row-major, floats 0-8), H2 (floats 9-17), 2 pad.
+    const float h1[9] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x};
+    const float h2[9] = {c.y, c.z, c.w, d.x, d.y, d.z, d.w, e.x, e.y};
+    const float s = 1.0f / (depth * scale);
+    float t[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) t[i] = fmaf(-s, h2[i], h1[i]);
+    WarpSetup w;
+    w.c0x = t[0]; w.c0y = t[3]; w.c0z = t[6];
+    w.c1x = t[1]; w.c1y = t[4]; w.c1z = t[7];
+    w.bx = fmaf(t[0], ox, fmaf(t[1], oy, t[2]));
+    w.by = fmaf(t[3], ox, fmaf(t[4], oy, t[5]));
+    w.bz = fmaf(t[6], ox, fmaf(t[7], oy, t[8]));
+    return w;
+}
+
+// Two windowed NCC evaluations (views va/vb at depths da/db) for one pixel; every lane
+// returns both results. Interleaving two evaluations doubles the independent fetches per
+// lane.
+template <int W>
+__device__ __forceinline__ void eval_pair(const RefDesc &D, const PixelWindow<W> &pw,
+                                          const float (&fdx)[Window<W>::NS],
+                                          const float (&fdy)[Window<W>::NS], int va, float da,
+                                          int vb, float db, float &out_a, float &out_b)
+{
+    constexpr int NS = Window<W>::NS;
+    const WarpSetup A = warp_setup(D, va, da, pw.scale, pw.ox, pw.oy);
+    const WarpSetup B = warp_setup(D, vb, db, pw.scale, pw.ox, pw.oy);
+    const cudaTextureObject_t ta = D.tex[va], tb = D.tex[vb];
+    const float swa = D.src_w[va], sha = D.src_h[va], swb = D.src_w[vb], shb = D.src_h[vb];
+    float ja = 0.f, jja = 0.f, ija = 0.f, jb = 0.f, jjb = 0.f, ijb = 0.f;
+#pragma unroll
+    for (int i = 0; i < NS; ++i) {
+        if (pw.inb & ((uint64_t)1 << i)) {
+            const float dx = fdx[i], dy = fdy[i];
+            const float pxa = fmaf(A.c0x, dx, fmaf(A.c1x, dy, A.bx));
+            const float pya = fmaf(A.c0y, dx, fmaf(A.c1y, dy, A.by));
+            const float pza = fmaf(A.c0z, dx, fmaf(A.c1z, dy, A.bz));
+            const float pxb = fmaf(B.c0x, dx, fmaf(B.c1x, dy, B.bx));
+            const float pyb = fmaf(B.c0y, dx, fmaf(B.c1y, dy, B.by));
+            const float pzb = fmaf(B.c0z, dx, fmaf(B.c1z, dy, B.bz));
+            const float ra = __fdividef(1.0f, pza), rb = __fdividef(1.0f, pzb);
+            const float sa = sample_source(ta, pxa * ra, pya * ra, swa, sha);
+            const float sb = sample_source(tb, pxb * rb, pyb * rb, swb, shb);
+            const float r = pw.rv[i];
+            ja += sa; jja = fmaf(sa, sa, jja); ija = fmaf(r, sa, ija);
+            jb += sb; jjb = fmaf(sb, sb, jjb); ijb = fmaf(r, sb, ijb);
+        }
+    }
+    ja = warp_sum(ja); jja = warp_sum(jja); ija = warp_sum(ija);
+    jb = warp_sum(jb); jjb = warp_sum(jjb); ijb = warp_sum(ijb);
+    out_a = ncc_finalize(ja, jja, ija, pw.si, pw.sii, pw.n);
+    out_b = ncc_finalize(jb, jjb, ijb, pw.si, pw.sii, pw.n);
+}
+
+// Per-lane slot offsets (dx, dy) of the window.
+template <int W>
+__device__ __forceinline__ void slot_offsets(int lane, float (&fdx)[Window<W>::NS],
+                                             float (&fdy)[Window<W>::NS])
+{
+#pragma unroll
+    for (int i = 0; i < Window<W>::NS; ++i) {
+        const int k = lane + 32 * i;
+        fdx[i] = (float)(k % W);
+        fdy[i] = (float)(k / W);
+    }
+}
+
+}  // namespace pm

@@ -1,0 +1,60 @@
+// pm_internal.h -- host-side declarations shared by the engine's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pm_sweep.cuh"
+
+namespace pm {
+
+enum class LaunchKind { Sweep, Costs, Eval };
+
+struct LaunchReq {
+    LaunchKind kind;
+    cudaStream_t stream;
+    int grid;
+    // Sweep
+    const SweepArgs *sweep;
+    // Costs / Eval
+    const RefDesc *refs;
+    int ref_index;
+    int axis;
+    int n;
+    const int4 *queries;
+    const float *depths;
+    float *out;
+};
+
+// Window-size dispatch, split over translation units so they compile in parallel.
+// Each returns cudaErrorInvalidValue when W is not in its group.
+cudaError_t launch_group_a(int W, const LaunchReq &req);  // 3 .. 11
+cudaError_t launch_group_b(int W, const LaunchReq &req);  // 13 .. 17
+cudaError_t launch_group_c(int W, const LaunchReq &req);  // 19 .. 25
+cudaError_t launch_group_d(int W, const LaunchReq &req);  // 27 .. 45
+
+inline cudaError_t launch_window(int W, const LaunchReq &req)
+{
+    if (W <= 11) return launch_group_a(W, req);
+    if (W <= 17) return launch_group_b(W, req);
+    if (W <= 25) return launch_group_c(W, req);
+    return launch_group_d(W, req);
+}
+
+// Prefilter, moments, conversions, init, transpose, Philox (pm_prep.cu).
+cudaError_t launch_u8_to_float(const uint8_t *in, int in_pitch, float *out, int w, int h,
+                               cudaStream_t s);
+cudaError_t launch_filter(const float *in, float *tmp, float *out, int w, int h, int radius,
+                          const float *weights, cudaStream_t s);
+cudaError_t launch_box_moments(const float *img, float *row_i, float *row_ii, float *sum_i,
+                               float *sum_ii, int w, int h, int hw, cudaStream_t s);
+cudaError_t launch_float_to_half(const float *in, void *out, int n, cudaStream_t s);
+cudaError_t launch_init_depth(const RefDesc *refs, int r, int npix, cudaStream_t s);
+cudaError_t launch_sample(const RefDesc *refs, int r, int view, int n, const float *xs,
+                          const float *ys, float *out, cudaStream_t s);
+cudaError_t launch_transpose(const float *in, size_t in_pitch, float *out, size_t out_pitch,
+                             int w, int h, int layers, cudaStream_t s);
+cudaError_t launch_philox(uint64_t seed, int n, const uint32_t *ctr, uint32_t *out,
+                          cudaStream_t s);
+
+}  // namespace pm

@@ -1,0 +1,198 @@
+// pm_prep.cu -- per-handle preparation kernels and small utilities.
+//
+//  u8 -> float texels (cudaReadModeNormalizedFloat of patchMatch.cu:27-28 made explicit),
+//  separable prefilter (GaussianBlurCUDA.cu:39-70), reference-window box moments
+//  (array2d_refImg.cu:11-67), FP16 texel conversion, random initial depth
+//  (array2d_wrapper.cu:3-20), source sampling queries, the layered transpose
+//  (cudaTranspose.h:9-46) and raw Philox output.
+#include <cuda_fp16.h>
+
+#include "pm_internal.h"
+
+namespace pm {
+
+namespace {
+
+constexpr int MAX_FILTER_TAPS = 45;
+struct FilterTaps {
+    float w[MAX_FILTER_TAPS];
+};
+
+__global__ void u8_to_float_kernel(const uint8_t *__restrict__ in, int in_pitch,
+                                   float *__restrict__ out, int w, int h)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x < w && y < h) out[(size_t)y * w + x] = (float)in[(size_t)y * in_pitch + x] / 255.0f;
+}
+
+// One 1-D pass of the separable filter with zero border; dir 0 = along x, 1 = along y.
+// Taps are applied in the reference's order (k = -radius .. radius, weight[radius - k]).
+__global__ void filter_pass_kernel(const float *__restrict__ in, float *__restrict__ out, int w,
+                                   int h, int radius, int dir, const FilterTaps taps)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= w || y >= h) return;
+    float s = 0.0f;
+    for (int k = -radius; k <= radius; ++k) {
+        const int xx = dir == 0 ? x + k : x, yy = dir == 0 ? y : y + k;
+        const float v = (xx >= 0 && xx < w && yy >= 0 && yy < h) ? in[(size_t)yy * w + xx] : 0.0f;
+        s += v * taps.w[radius - k];
+    }
+    out[(size_t)y * w + x] = s;
+}
+
+__global__ void box_rows_kernel(const float *__restrict__ img, float *__restrict__ ri,
+                                float *__restrict__ rii, int w, int h, int hw)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= w || y >= h) return;
+    float a = 0.0f, b = 0.0f;
+    for (int k = -hw; k <= hw; ++k) {
+        const int xx = x + k;
+        const float v = (xx >= 0 && xx < w) ? img[(size_t)y * w + xx] : 0.0f;
+        a += v;
+        b += v * v;
+    }
+    ri[(size_t)y * w + x] = a;
+    rii[(size_t)y * w + x] = b;
+}
+
+__global__ void box_cols_kernel(const float *__restrict__ ri, const float *__restrict__ rii,
+                                float *__restrict__ si, float *__restrict__ sii, int w, int h,
+                                int hw)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= w || y >= h) return;
+    float a = 0.0f, b = 0.0f;
+    for (int k = -hw; k <= hw; ++k) {
+        const int yy = y + k;
+        if (yy < 0 || yy >= h) continue;
+        a += ri[(size_t)yy * w + x];
+        b += rii[(size_t)yy * w + x];
+    }
+    si[(size_t)y * w + x] = a;
+    sii[(size_t)y * w + x] = b;
+}
+
+__global__ void float_to_half_kernel(const float *__restrict__ in, __half *__restrict__ out, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = __float2half_rn(in[i]);
+}
+
+__global__ void init_depth_kernel(const RefDesc *refs, int r, int npix)
+{
+    const RefDesc &D = refs[r];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npix) return;
+    const float u = draw_uniform(D.seed, (uint32_t)i, INIT_SWEEP_ID, RNG_INIT, 0, D.batch_id);
+    D.depth[i] = (1.0f - u) * D.depth_span + D.depth_near;
+}
+
+__global__ void sample_kernel(const RefDesc *refs, int r, int view, int n,
+                              const float *__restrict__ xs, const float *__restrict__ ys,
+                              float *__restrict__ out)
+{
+    const RefDesc &D = refs[r];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = sample_source(D.tex[view], xs[i], ys[i], D.src_w[view], D.src_h[view]);
+}
+
+// 32x32 shared tile with one column of padding against bank conflicts; blockIdx.z = layer.
+__global__ void transpose_kernel(const float *__restrict__ in, size_t in_pitch,
+                                 float *__restrict__ out, size_t out_pitch, int w, int h)
+{
+    __shared__ float tile[32][33];
+    const int layer = blockIdx.z;
+    const float *lin = (const float *)((const char *)in + (size_t)layer * h * in_pitch);
+    float *lout = (float *)((char *)out + (size_t)layer * w * out_pitch);
+    const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+    for (int j = threadIdx.y; j < 32; j += 8) {
+        const int x = bx + threadIdx.x, y = by + j;
+        if (x < w && y < h) tile[j][threadIdx.x] = *(const float *)((const char *)lin + (size_t)y * in_pitch + (size_t)x * 4);
+    }
+    __syncthreads();
+    for (int j = threadIdx.y; j < 32; j += 8) {
+        const int ox = by + threadIdx.x, oy = bx + j;  // output column = input row
+        if (ox < h && oy < w) *(float *)((char *)lout + (size_t)oy * out_pitch + (size_t)ox * 4) = tile[threadIdx.x][j];
+    }
+}
+
+__global__ void philox_kernel(uint64_t seed, int n, const uint4 *__restrict__ ctr,
+                              uint4 *__restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = philox4x32_10(ctr[i], make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)));
+}
+
+inline dim3 grid2d(int w, int h, dim3 b) { return dim3((w + b.x - 1) / b.x, (h + b.y - 1) / b.y); }
+
+}  // namespace
+
+cudaError_t launch_u8_to_float(const uint8_t *in, int in_pitch, float *out, int w, int h,
+                               cudaStream_t s)
+{
+    const dim3 b(32, 8);
+    u8_to_float_kernel<<<grid2d(w, h, b), b, 0, s>>>(in, in_pitch, out, w, h);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_filter(const float *in, float *tmp, float *out, int w, int h, int radius,
+                          const float *weights, cudaStream_t s)
+{
+    if (radius < 0 || 2 * radius + 1 > MAX_FILTER_TAPS) return cudaErrorInvalidValue;
+    FilterTaps taps{};
+    for (int i = 0; i < 2 * radius + 1; ++i) taps.w[i] = weights[i];
+    const dim3 b(32, 8);
+    filter_pass_kernel<<<grid2d(w, h, b), b, 0, s>>>(in, tmp, w, h, radius, 0, taps);
+    filter_pass_kernel<<<grid2d(w, h, b), b, 0, s>>>(tmp, out, w, h, radius, 1, taps);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_box_moments(const float *img, float *row_i, float *row_ii, float *sum_i,
+                               float *sum_ii, int w, int h, int hw, cudaStream_t s)
+{
+    const dim3 b(32, 8);
+    box_rows_kernel<<<grid2d(w, h, b), b, 0, s>>>(img, row_i, row_ii, w, h, hw);
+    box_cols_kernel<<<grid2d(w, h, b), b, 0, s>>>(row_i, row_ii, sum_i, sum_ii, w, h, hw);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_float_to_half(const float *in, void *out, int n, cudaStream_t s)
+{
+    float_to_half_kernel<<<(n + 255) / 256, 256, 0, s>>>(in, (__half *)out, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_init_depth(const RefDesc *refs, int r, int npix, cudaStream_t s)
+{
+    init_depth_kernel<<<(npix + 255) / 256, 256, 0, s>>>(refs, r, npix);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sample(const RefDesc *refs, int r, int view, int n, const float *xs,
+                          const float *ys, float *out, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    sample_kernel<<<(n + 255) / 256, 256, 0, s>>>(refs, r, view, n, xs, ys, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_transpose(const float *in, size_t in_pitch, float *out, size_t out_pitch,
+                             int w, int h, int layers, cudaStream_t s)
+{
+    if (w <= 0 || h <= 0 || layers <= 0 || layers > 65535) return cudaErrorInvalidValue;
+    transpose_kernel<<<dim3((w + 31) / 32, (h + 31) / 32, layers), dim3(32, 8), 0, s>>>(
+        in, in_pitch, out, out_pitch, w, h);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_philox(uint64_t seed, int n, const uint32_t *ctr, uint32_t *out,
+                          cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    philox_kernel<<<(n + 255) / 256, 256, 0, s>>>(seed, n, (const uint4 *)ctr, (uint4 *)out);
+    return cudaGetLastError();
+}
+
+}  // namespace pm

@@ -1,0 +1,4 @@
+// Window sides 3..11 of the window-templated kernels.
+#define PM_GROUP_FN launch_group_a
+#define PM_WINDOW_LIST(X) X(3) X(5) X(7) X(9) X(11)
+#include "pm_windows.inc"

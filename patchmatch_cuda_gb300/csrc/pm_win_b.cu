@@ -1,0 +1,4 @@
+// Window sides 13..17 of the window-templated kernels.
+#define PM_GROUP_FN launch_group_b
+#define PM_WINDOW_LIST(X) X(13) X(15) X(17)
+#include "pm_windows.inc"

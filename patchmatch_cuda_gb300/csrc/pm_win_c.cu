@@ -1,0 +1,4 @@
+// Window sides 19..25 of the window-templated kernels.
+#define PM_GROUP_FN launch_group_c
+#define PM_WINDOW_LIST(X) X(19) X(21) X(23) X(25)
+#include "pm_windows.inc"

@@ -1,0 +1,207 @@
+"""Parity of the CUDA kernels against the CPU oracle, stage by stage (needs a GPU).
+
+Tolerances: source sampling 2e-6 absolute (FP32 weights vs FP64), NCC 1e-4 absolute (the
+spec bound; FP32 engine vs FP64 oracle), box moments 1e-5 relative, Philox bit-exact.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def bilinear_ref(img, xs, ys):
+    """Exact bilinear at (xs, ys), texel i at coordinate i, zero border (float64)."""
+    h, w = img.shape
+    out = np.zeros(xs.shape, np.float64)
+    for i, (x, y) in enumerate(zip(xs.astype(np.float64), ys.astype(np.float64))):
+        if not (-1 < x < w and -1 < y < h):
+            continue
+        x0, y0 = int(np.floor(x)), int(np.floor(y))
+        ax, ay = x - x0, y - y0
+
+        def t(a, b):
+            return float(img[b, a]) if 0 <= a < w and 0 <= b < h else 0.0
+        out[i] = ((1 - ax) * (1 - ay) * t(x0, y0) + ax * (1 - ay) * t(x0 + 1, y0)
+                  + (1 - ax) * ay * t(x0, y0 + 1) + ax * ay * t(x0 + 1, y0 + 1))
+    return out
+
+
+@pytest.fixture(scope="module")
+def small_scene():
+    from patchmatch_cuda_gb300 import scene
+    w = scene.WORKLOADS["plane3_320x240"]
+    return scene.make_views(w)
+
+
+def make_engine(sv, **over):
+    from patchmatch_cuda_gb300 import Engine
+    return Engine(sv.images, sv.ref_id, sv.workload.params(**over))
+
+
+def oracle_for(eng, sv, params=None):
+    from oracle import pm_oracle
+    src = [eng.source_texels(v) for v in range(eng.n_src)]
+    ref, si, sii = eng.ref_maps()
+    return pm_oracle.from_images(sv.images, sv.ref_id, params or eng.params, source_texels=src, ref_texels=ref)
+
+
+@pytest.mark.parametrize("prefilter,precision", [(0, 0), (1, 0), (1, 1)])
+def test_source_sampling_exact_bilinear(small_scene, prefilter, precision):
+    eng = make_engine(small_scene, prefilter=prefilter, precision=precision)
+    rng = np.random.default_rng(1)
+    tex = eng.source_texels(1)
+    h, w = tex.shape
+    xs = rng.uniform(-3, w + 2, 3000).astype(np.float32)
+    ys = rng.uniform(-3, h + 2, 3000).astype(np.float32)
+    xs[:50] = np.arange(50, dtype=np.float32)  # exact texel positions
+    ys[:50] = 7.0
+    got = eng.sample_source(1, xs, ys)
+    want = bilinear_ref(tex, xs, ys)
+    np.testing.assert_allclose(got, want, atol=2e-6, rtol=0)
+    eng.close()
+
+
+def test_u8_texels_are_unorm(small_scene):
+    eng = make_engine(small_scene, prefilter=0)
+    src = [im for i, im in enumerate(small_scene.images) if i != small_scene.ref_id][0]
+    np.testing.assert_array_equal(eng.source_texels(0), src.image.astype(np.float32) / np.float32(255))
+    ref, _, _ = eng.ref_maps()
+    np.testing.assert_array_equal(ref, small_scene.images[small_scene.ref_id].image.astype(np.float32) / np.float32(255))
+    eng.close()
+
+
+def test_reference_moments_and_prefilter(small_scene):
+    from oracle import pm_oracle
+    eng = make_engine(small_scene, prefilter=1)
+    ref, si, sii = eng.ref_maps()
+    raw = small_scene.images[small_scene.ref_id].image.astype(np.float32) / np.float32(255)
+    want_ref = pm_oracle.prefilter(raw, 1, 1.0)
+    np.testing.assert_allclose(ref, want_ref, rtol=1e-6, atol=1e-6)
+    osi, osii = pm_oracle.box_moments(ref, small_scene.workload.half_window)
+    np.testing.assert_allclose(si, osi, rtol=1e-5, atol=1e-5)
+    np.testing.assert_allclose(sii, osii, rtol=1e-5, atol=1e-5)
+    eng.close()
+
+
+@pytest.mark.parametrize("quirks", [1, 0])
+def test_ncc_parity(small_scene, quirks):
+    eng = make_engine(small_scene, quirks=quirks)
+    orc = oracle_for(eng, small_scene)
+    rng = np.random.default_rng(2)
+    n = 4096
+    w = small_scene.workload
+    xs = rng.integers(0, w.width, n)
+    ys = rng.integers(0, w.height, n)
+    xs[:256] = rng.integers(0, w.half_window + 1, 256)  # leading edges, where the quirk acts
+    ys[256:512] = rng.integers(0, w.half_window + 1, 256)
+    vs = rng.integers(0, w.n_src, n)
+    gt = small_scene.gt_depth[ys, xs]
+    ds = np.where(rng.random(n) < 0.5, gt, rng.uniform(w.depth_near, w.depth_far, n)).astype(np.float32)
+    ax = rng.integers(0, 2, n)
+    got = eng.eval_costs(xs, ys, vs, ds, ax)
+    want = orc.ncc_batch(xs, ys, vs, ds, ax)
+    err = np.abs(got - want)
+    assert err.max() <= 1e-4, f"max |NCC_gpu - NCC_oracle| = {err.max():.3g}"
+    eng.close()
+
+
+def kat_views(kind):
+    """Reference plus one source whose principal point is shifted by half a pixel, so the
+    plane-induced homography maps reference pixel centre i + 1/2 onto source texel i."""
+    from patchmatch_cuda_gb300 import Image
+    rng = np.random.default_rng(4)
+    ref = rng.integers(0, 256, (40, 48)).astype(np.uint8)
+    if kind == "identical":
+        src = ref.copy()
+    elif kind == "flat":
+        ref = np.full_like(ref, 90)
+        src = ref.copy()
+    else:  # black source
+        src = np.zeros_like(ref)
+    K = np.array([[50.0, 0, 24], [0, 50.0, 20], [0, 0, 1]])
+    Ks = K.copy()
+    Ks[0, 2] -= 0.5
+    Ks[1, 2] -= 0.5
+    I3, z = np.eye(3), np.zeros(3)
+    return [Image(K, I3, z, ref), Image(Ks, I3, z, src)]
+
+
+@pytest.mark.parametrize("kind,expected", [("identical", 0.0), ("flat", 1.0), ("black", 2.0)])
+def test_ncc_known_answers(kind, expected):
+    from patchmatch_cuda_gb300 import Engine, default_params
+    p = default_params()
+    p.depth_near, p.depth_far, p.half_window = 1.0, 10.0, 3
+    eng = Engine(kat_views(kind), 0, p)
+    xs, ys = np.meshgrid(np.arange(3, 45), np.arange(3, 37))
+    xs, ys = xs.ravel(), ys.ravel()
+    got = eng.eval_costs(xs, ys, np.zeros_like(xs), np.full(xs.shape, 4.0, np.float32), 0)
+    np.testing.assert_allclose(got, expected, atol=1e-5)
+    eng.close()
+
+
+def test_philox_matches_oracle(engine_lib):
+    import ctypes as C
+    from oracle import pm_oracle
+    rng = np.random.default_rng(3)
+    ctr = rng.integers(0, 2**32, (257, 4), dtype=np.uint64).astype(np.uint32)
+    out = np.zeros_like(ctr)
+    seed = 0x1234_5678_9ABC_DEF0
+    assert engine_lib.pm_philox(seed, len(ctr), ctr.ctypes.data, out.ctypes.data) == 0
+    key = np.array([seed & 0xFFFFFFFF, seed >> 32], np.uint32)
+    for i in range(len(ctr)):
+        np.testing.assert_array_equal(out[i], pm_oracle.philox(ctr[i], key))
+
+
+def test_initial_depth_and_costs_match_oracle(small_scene):
+    eng = make_engine(small_scene)
+    orc = oracle_for(eng, small_scene)
+    eng.init_depth()
+    d = eng.depth()
+    od = orc.init_depth()
+    np.testing.assert_allclose(d, od, rtol=2e-7, atol=1e-6)
+    eng.compute_costs(1)
+    c = eng.costs()
+    oc = orc.initial_costs(d.astype(np.float64))
+    err = np.abs(c - oc)
+    assert err.max() <= 1e-4, f"max cost error {err.max():.3g}"
+    eng.close()
+
+
+@pytest.mark.parametrize("direction", [0, 1, 2, 3])
+def test_sweep_lockstep(small_scene, direction):
+    """One sweep from the same state: decisions agree almost everywhere, costs to 1e-4."""
+    eng = make_engine(small_scene)
+    orc = oracle_for(eng, small_scene)
+    eng.init_depth()
+    eng.compute_costs(1)
+    d0 = eng.depth().astype(np.float64)
+    c0 = eng.costs().astype(np.float64)
+    S = small_scene.workload.num_samples
+    eng.run_sweep(direction, 4 + direction, S)
+    gd, gc = eng.depth(), eng.costs()
+    od, oc = d0.copy(), c0.copy()
+    orc.sweep(od, oc, direction, 4 + direction, S)
+    same = np.abs(gd - od) <= 1e-6 * np.abs(od)
+    assert same.mean() >= 0.995, f"depth agreement {same.mean():.4f}"
+    cerr = np.abs(gc - oc)[same]
+    assert np.quantile(cerr, 0.999) <= 1e-4, f"cost error q999 {np.quantile(cerr, 0.999):.3g}"
+    eng.close()
+
+
+def test_full_run_matches_oracle(small_scene):
+    from patchmatch_cuda_gb300 import scene
+    eng = make_engine(small_scene)
+    orc = oracle_for(eng, small_scene)
+    eng.run()
+    gd = eng.depth()
+    w = small_scene.workload
+    od, oc, ovs, n = orc.run(w.iterations, w.num_samples)
+    rel = np.abs(gd - od) / od
+    frac = float(np.mean(rel <= 1e-3))
+    bad_g = scene.bad_pixel_rate(gd, small_scene.gt_depth)
+    bad_o = scene.bad_pixel_rate(od.astype(np.float32), small_scene.gt_depth)
+    assert abs(bad_g - bad_o) <= 0.01, (bad_g, bad_o)
+    assert frac >= 0.95, f"only {frac:.4f} of depths within 0.1% of the oracle"
+    st = eng.stats()
+    assert st.cost_evals > 0
+    eng.close()
