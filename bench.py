@@ -1,0 +1,383 @@
+#!/usr/bin/env python3
+"""PatchMatch MVS depth-map benchmark on one GPU per rank.
+
+One step = one complete depth map (random init, initial costs, iterations x 4 sweeps) of the
+1280x720 reference with 10 source views, 15x15 window, 5 iterations (box200_1280x720: a seeded
+synthetic scene of 12 planes and 200 boxes standing in for the benchmark's data). The metric is
+G cost-evals/s: NCC evaluations of one (pixel, hypothesis, source view) over the w x w window,
+counted as the reference algorithm performs them.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU restatement of the same algorithm (FP32, all host threads) on a
+bounded sample of the same workload; the reference's own CUDA build does not compile with
+CUDA 13 (texture references) and needs OpenCV and Boost.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+CLOCK_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="box200_1280x720")
+    ap.add_argument("--precision", type=int, default=0, help="0 = FP32, 1 = FP16 texels (mixed)")
+    ap.add_argument("--cpu-seconds", type=float, default=8.0, help="CPU baseline sample budget")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while active."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={CLOCK_FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        rows = []
+        try:
+            for line in Path(self.path).read_text().splitlines():
+                f = [x.strip() for x in line.split(",")]
+                if len(f) >= 9 and f[1].replace(".", "").isdigit():
+                    rows.append(f)
+        finally:
+            try:
+                os.unlink(self.path)
+            except OSError:
+                pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[1]) for r in rows]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": float(rows[0][2]), "reasons": reasons,
+                "samples": len(rows), "power_w_max": max(float(r[3]) for r in rows if r[3].replace(".", "").isdigit())}
+
+
+def dist_setup(use_cuda: bool):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if use_cuda else "gloo")
+    return world, rank, local
+
+
+def allreduce_max_sum(world: int, vmax: float, vsum: float):
+    if world == 1:
+        return vmax, vsum
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([vmax], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    s = torch.tensor([vsum], dtype=torch.float64, device=dev)
+    dist.all_reduce(s, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(s.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except ValueError:
+            pass
+    return {}
+
+
+def profiled_traffic(workload: str):
+    """DRAM bytes per sweep launch from the committed ncu summary, if one exists."""
+    f = ROOT / "profiles" / f"sweep_kernel_{workload}.txt"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.startswith("dram_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_baseline(eng, sv, wl, seconds: float) -> dict:
+    """The FP32 CPU restatement on a bounded sample: lines of one top-to-bottom sweep from the
+    engine's initial state, on all host threads."""
+    import numpy as np
+    from oracle import pm_oracle
+    eng.init_depth()
+    eng.compute_costs(1)
+    d0 = eng.depth().astype(np.float64)
+    c0 = eng.costs().astype(np.float64)
+    src = [eng.source_texels(v) for v in range(eng.n_src)]
+    ref, _, _ = eng.ref_maps()
+    orc = pm_oracle.from_images(sv.images, sv.ref_id, eng.params, source_texels=src, ref_texels=ref, fp32=True)
+    S = wl.num_samples
+    lines, evals, elapsed = 8, 0, 0.0
+    while True:
+        d, c = d0.copy(), c0.copy()
+        t = time.perf_counter()
+        n = orc.sweep(d, c, 1, 1, S, lines=(0, lines))
+        dt = time.perf_counter() - t
+        if dt >= 0.25 * seconds or lines >= wl.width:
+            evals, elapsed = n, dt
+            break
+        lines = min(wl.width, max(lines * 2, int(lines * 0.3 * seconds / max(dt, 1e-3))))
+    return {"value": evals / elapsed / 1e9, "unit": "G cost-evals/s", "cores": pm_oracle.num_threads(True),
+            "kind": "port", "seconds": round(elapsed, 3),
+            "sample": f"{lines} of {wl.width} lines of one top-to-bottom sweep, S={S}, FP32, "
+                      f"from the engine's initial state ({evals} cost-evals)"}
+
+
+def run_reference(args):
+    """The CPU restatement (FP32, all host threads): each step sweeps a bounded sample of lines
+    of the workload's top-to-bottom sweep from a random initial state."""
+    if int(os.environ.get("RANK", "0")) != 0:
+        return 0
+    from oracle import pm_oracle
+    from patchmatch_cuda_gb300 import scene
+    wl = scene.WORKLOADS[args.workload]
+    sv = scene.make_views(wl)
+    orc = pm_oracle.from_images(sv.images, sv.ref_id, _plain_params(wl), fp32=True)
+    depth0 = orc.init_depth()
+    S = wl.num_samples
+    lines = 16
+    cost0 = _sample_costs(orc, depth0, lines)
+    times, evals = [], []
+    for step in range(args.warmup + args.steps):
+        d, c = depth0.copy(), cost0.copy()
+        t0 = time.perf_counter()
+        n = orc.sweep(d, c, 1, 1, S, lines=(0, lines))
+        dt = time.perf_counter() - t0
+        if step >= args.warmup:
+            times.append(dt)
+            evals.append(n)
+    value = sum(evals) / sum(times) / 1e9
+    sample = f"{lines} of {wl.width} lines of one top-to-bottom sweep per step, S={S}, FP32"
+    print(json.dumps({
+        "impl": "reference", "metric": "G cost-evals/s", "value": value, "unit": "G cost-evals/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": args.workload},
+        "cpu_baseline": {"value": value, "unit": "G cost-evals/s", "cores": pm_oracle.num_threads(True),
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "G cost-evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+    return 0
+
+
+def _engine_available() -> bool:
+    try:
+        from patchmatch_cuda_gb300 import _native
+        _native.load_engine()
+        return True
+    except Exception:
+        return False
+
+
+def _plain_params(wl):
+    from patchmatch_cuda_gb300 import PmParams
+    p = PmParams()
+    p.depth_near, p.depth_far, p.half_window = wl.depth_near, wl.depth_far, wl.half_window
+    p.num_samples, p.sp_alpha, p.gaussian_sigma = wl.num_samples, wl.sp_alpha, wl.gaussian_sigma
+    p.prefilter, p.num_iterations, p.orientation_x, p.orientation_z = wl.prefilter, wl.iterations, 0.0, 1.0
+    p.seed, p.quirks = wl.seed, 1
+    return p
+
+
+def _sample_costs(orc, depth, cols):
+    """Initial costs (every view at the initial depth) for the first `cols` columns, the only
+    ones a sweep over those lines touches; other entries are unused."""
+    import numpy as np
+    c = np.ones((orc.H, orc.W, orc.V), np.float64)
+    xs, ys = np.meshgrid(np.arange(min(cols, orc.W)), np.arange(orc.H))
+    xs, ys = xs.ravel(), ys.ravel()
+    for v in range(orc.V):
+        c[ys, xs, v] = orc.ncc_batch(xs, ys, np.full(xs.shape, v), depth[ys, xs], 1)
+    return c
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    world, rank, local = dist_setup(True)
+    torch.cuda.set_device(local)
+    from patchmatch_cuda_gb300 import Engine, _native, scene
+    from patchmatch_cuda_gb300 import build as engine_build
+    if not _native.ENGINE_PATH.exists():
+        engine_build.build()
+    wl = scene.WORKLOADS[args.workload]
+    sv = scene.make_views(wl, seed=wl.seed + rank)  # each rank its own reference view (replicas)
+    params = wl.params(precision=args.precision, gpu_id=local)
+    eng = Engine(sv.images, sv.ref_id, params)
+    stream = torch.cuda.ExternalStream(eng.stream())
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+
+    for _ in range(max(args.warmup, 0)):
+        eng.run()
+    evals_per_map = eng.stats().cost_evals
+    launches_per_map = 2 + 4 * wl.iterations
+
+    barrier(world)
+    torch.cuda.synchronize()
+    step_ms = []
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            eng.run_async()
+            e1.record(stream)
+            e1.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+    torch.cuda.synchronize()
+    barrier(world)
+    total_ms, total_evals = allreduce_max_sum(world, sum(step_ms), float(evals_per_map * args.steps))
+    depth = eng.depth()
+    bad = scene.bad_pixel_rate(depth, sv.gt_depth)
+
+    # dominant kernel: every sweep of one schedule timed on the engine's stream
+    eng.init_depth()
+    eng.compute_costs(1)
+    sweep_ms, sweep_evals = [], []
+    prev = eng.stats().cost_evals
+    for it in range(wl.iterations):
+        for d in range(4):
+            eng.run_sweep(d, 4 * it + d, 1 if it == 0 else wl.num_samples)
+            st = eng.stats()
+            sweep_ms.append(st.ms_sweeps)
+            sweep_evals.append(st.cost_evals - prev)
+            prev = st.cost_evals
+    w = 2 * wl.half_window + 1
+    flop_per_eval = 16 * w * w + 36
+    launch_s = 1e-3 * sum(sweep_ms) / len(sweep_ms)
+    flop_per_launch = flop_per_eval * sum(sweep_evals) / len(sweep_evals)
+    props = torch.cuda.get_device_properties(local)
+    peaks = measured_peaks()
+    sm_max = float(peaks.get("sm_max_mhz", 2070.0))
+    fp32_peak = props.multi_processor_count * 128 * 2 * sm_max * 1e6 / 1e12
+    achieved = flop_per_launch / launch_s / 1e12
+    samples_per_s = (flop_per_launch / flop_per_eval) * w * w / launch_s
+    tex_peak = props.multi_processor_count * 4 * sm_max * 1e6
+
+    # end to end through the C ABI with host buffers: create (upload, prefilter, textures),
+    # run, read the depth map back, destroy
+    h2d = sum(im.image.nbytes for im in sv.images)
+    d2h = wl.width * wl.height * 4
+    e2e_times = []
+    for i in range(1 + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e = Engine(sv.images, sv.ref_id, params)
+        e.run()
+        _ = e.depth()
+        e.close()
+        torch.cuda.synchronize()
+        if i > 0:
+            e2e_times.append(time.perf_counter() - t0)
+    e2e_max, _ = allreduce_max_sum(world, sum(e2e_times), 0.0)
+    e2e_value = total_evals / e2e_max / 1e9
+
+    tpl = eng.stats().threads_per_line
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(eng, sv, wl, args.cpu_seconds)
+    eng.close()
+
+    if rank == 0:
+        traffic = profiled_traffic(args.workload)
+        out = {
+            "metric": "G cost-evals/s", "value": total_evals / (total_ms * 1e-3) / 1e9, "unit": "G cost-evals/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32" if args.precision == 0 else "f16 texels, f32 moments",
+            "data": "synthetic (seeded scene: 12 planes + 200 boxes, 1 ref + 10 sources on a 15 degree arc)",
+            "config": {
+                "workload": args.workload, "width": wl.width, "height": wl.height, "n_src": wl.n_src,
+                "window": w, "iterations": wl.iterations, "num_samples": wl.num_samples,
+                "prefilter": "box, sigma 1", "precision": "fp32" if args.precision == 0 else "mixed",
+                "ms_per_depth_map": total_ms / args.steps, "cost_evals_per_depth_map": evals_per_map,
+                "bad_pixel_pct_1pct": round(100 * bad, 3),
+                "l2": "flushed before each depth map (256 MiB write, outside the timed events)",
+                "threads_per_line": tpl,
+            },
+            "roofline": {
+                "bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                "frac": achieved / fp32_peak, "traffic": traffic,
+                "kernel": "sweep_kernel", "launch_ms": 1e3 * launch_s,
+                "flop_per_launch": flop_per_launch,
+                "peak_source": "nominal FP32: SMs x 128 lanes x 2 x sm_max_mhz (MEASURED_PEAKS.json has no FP32 figure)",
+                "tex_samples_per_s": samples_per_s, "tex_peak_samples_per_s": tex_peak,
+                "tex_frac": samples_per_s / tex_peak,
+            },
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "G cost-evals/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_max / args.steps},
+            "gpu_launches": launches_per_map * args.steps,
+            "clocks": clocks.summary(),
+        }
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -27,7 +27,7 @@ struct pm_handle {
     int texel_bytes = 4;
     std::string err;
 
-    float *d_ref = nullptr, *d_sum_i = nullptr, *d_sum_ii = nullptr;
+    float *d_ref = nullptr, *d_sum_i = nullptr, *d_sum_ii = nullptr, *d_c1 = nullptr;
     float *d_depth = nullptr, *d_cost = nullptr, *d_beta = nullptr;
     uint8_t *d_view_sel = nullptr;
     unsigned long long *d_evals = nullptr;
@@ -40,6 +40,7 @@ struct pm_handle {
     int src_w[MAX_VIEWS] = {}, src_h[MAX_VIEWS] = {};
     SweepArgs *h_sweep_args = nullptr;   // pinned, one per sweep of the schedule
 
+    int wpl[2] = {0, 0};                // warps per line: [vertical sweeps, horizontal sweeps]
     cudaGraphExec_t graph = nullptr;
     bool ran = false;
     pm_stats stats{};
@@ -214,7 +215,7 @@ cudaError_t enqueue_costs(pm_handle *h, int axis)
     req.ref_index = 0;
     req.axis = axis;
     const int npix = h->W * h->H;
-    req.grid = (npix + SWEEP_BLOCK / 32 - 1) / (SWEEP_BLOCK / 32);
+    req.grid = (npix + COST_BLOCK / 32 - 1) / (COST_BLOCK / 32);
     return launch_window(window_side(h), req);
 }
 
@@ -232,14 +233,47 @@ void fill_sweep_args(SweepArgs &a, const RefDesc *refs, const int *lines, int nr
     a.total_lines = a.line_start[nrefs];
 }
 
-cudaError_t enqueue_sweep(int win, const SweepArgs &a, cudaStream_t s)
+cudaError_t enqueue_sweep(int win, int wpl, const SweepArgs &a, cudaStream_t s)
 {
+    if (a.total_lines == 0) return cudaSuccess;
     LaunchReq req{};
     req.kind = LaunchKind::Sweep;
     req.stream = s;
     req.sweep = &a;
-    req.grid = (a.total_lines + SWEEP_BLOCK / 32 - 1) / (SWEEP_BLOCK / 32);
+    req.grid = a.total_lines;
+    req.block = 32 * wpl;
     return launch_window(win, req);
+}
+
+inline int orient(int dir) { return (dir == PM_DIR_LEFT_TO_RIGHT || dir == PM_DIR_RIGHT_TO_LEFT) ? 1 : 0; }
+
+// ---- warps-per-line tuner ----------------------------------------------------------------
+// A line's steps are sequential, so a sweep takes ceil(lines / resident lines) line-times;
+// more warps per line shorten a line-time but fit fewer lines. The tuner times one sweep
+// of the real workload for each candidate and remembers the winner per shape.
+struct TuneKey {
+    int device, win, n_src, num_samples, lines, steps, texel_bytes;
+    bool operator==(const TuneKey &o) const
+    {
+        return device == o.device && win == o.win && n_src == o.n_src && num_samples == o.num_samples &&
+               lines == o.lines && steps == o.steps && texel_bytes == o.texel_bytes;
+    }
+};
+std::mutex g_tune_mutex;
+std::vector<std::pair<TuneKey, int>> g_tuned;
+
+int tuned_lookup(const TuneKey &k)
+{
+    std::lock_guard<std::mutex> lk(g_tune_mutex);
+    for (auto &e : g_tuned)
+        if (e.first == k) return e.second;
+    return 0;
+}
+
+void tuned_store(const TuneKey &k, int wpl)
+{
+    std::lock_guard<std::mutex> lk(g_tune_mutex);
+    g_tuned.push_back({k, wpl});
 }
 
 int lines_of(const pm_handle *h, int dir)
@@ -263,10 +297,73 @@ cudaError_t enqueue_schedule(pm_handle *h)
             const int lines = lines_of(h, d);
             fill_sweep_args(a, h->d_desc, &lines, 1, d, (uint32_t)(4 * it + d), it == 0 ? 1 : 0,
                             (it == iters - 1 && d == PM_DIR_BOTTOM_TO_TOP) ? 1 : 0);
-            e = enqueue_sweep(window_side(h), a, h->stream);
+            e = enqueue_sweep(window_side(h), h->wpl[orient(d)], a, h->stream);
             if (e != cudaSuccess) return e;
         }
     return cudaSuccess;
+}
+
+// Picks warps per line for both sweep orientations: the caller's choice, a remembered
+// result, or timing candidates on the handle's own buffers (before the run initialises them).
+cudaError_t tune_warps_per_line(pm_handle *h)
+{
+    if (h->wpl[0] && h->wpl[1]) return cudaSuccess;
+    if (h->p.threads_per_line) {
+        h->wpl[0] = h->wpl[1] = h->p.threads_per_line / 32;
+        return cudaSuccess;
+    }
+    cudaError_t e = cudaSuccess;
+    bool state_ready = false;
+    for (int o = 0; o < 2; ++o) {
+        const int dir = o == 0 ? PM_DIR_TOP_TO_BOTTOM : PM_DIR_LEFT_TO_RIGHT;
+        const TuneKey key{h->device, h->win, h->V, h->p.num_samples, lines_of(h, dir),
+                          o == 0 ? h->H : h->W, h->texel_bytes};
+        int best = tuned_lookup(key);
+        if (!best) {
+            if (!state_ready) {
+                e = launch_init_depth(h->d_desc, 0, h->W * h->H, h->stream);
+                if (e == cudaSuccess) e = enqueue_costs(h, 1);
+                if (e != cudaSuccess) return e;
+                state_ready = true;
+            }
+            float best_ms = 1e30f;
+            for (int wpl = 1; wpl <= MAX_WARPS_PER_LINE; ++wpl) {
+                SweepArgs a;
+                const int lines = lines_of(h, dir);
+                fill_sweep_args(a, h->d_desc, &lines, 1, dir, 0xFFFFFFF0u, 0, 0);
+                float ms = 0.0f;
+                for (int rep = 0; rep < 2; ++rep) {  // first launch warms caches
+                    e = cudaEventRecord(h->ev[2], h->stream);
+                    if (e == cudaSuccess) e = enqueue_sweep(h->win, wpl, a, h->stream);
+                    if (e == cudaSuccess) e = cudaEventRecord(h->ev[3], h->stream);
+                    if (e == cudaSuccess) e = cudaEventSynchronize(h->ev[3]);
+                    if (e != cudaSuccess) return e;
+                    cudaEventElapsedTime(&ms, h->ev[2], h->ev[3]);
+                }
+                if (ms < best_ms) { best_ms = ms; best = wpl; }
+            }
+            tuned_store(key, best);
+        }
+        h->wpl[o] = best;
+    }
+    h->stats.threads_per_line = 32 * std::max(h->wpl[0], h->wpl[1]);
+    return cudaSuccess;
+}
+
+// Warps per line for a batched launch: the most that still keeps every line resident.
+int batch_wpl(int win, int total_lines, int device)
+{
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    for (int wpl = MAX_WARPS_PER_LINE; wpl > 1; --wpl) {
+        int occ = 0;
+        LaunchReq r{};
+        r.kind = LaunchKind::SweepOccupancy;
+        r.block = 32 * wpl;
+        r.occupancy = &occ;
+        if (launch_window(win, r) == cudaSuccess && total_lines <= occ * sms) return wpl;
+    }
+    return 1;
 }
 
 pm_status set_device(pm_handle *h)
@@ -322,7 +419,7 @@ pm_status pm_destroy(pm_handle *h)
         if (h->tex[v]) cudaDestroyTextureObject(h->tex[v]);
         if (h->arr[v]) release_array(h->device, h->src_w[v], h->src_h[v], h->texel_bytes, h->arr[v]);
     }
-    void *bufs[] = {h->d_ref, h->d_sum_i, h->d_sum_ii, h->d_depth, h->d_cost, h->d_beta,
+    void *bufs[] = {h->d_ref, h->d_sum_i, h->d_sum_ii, h->d_c1, h->d_depth, h->d_cost, h->d_beta,
                     h->d_view_sel, h->d_evals, h->d_hh, h->d_hh64, h->d_desc};
     for (void *b : bufs)
         if (b) cudaFreeAsync(b, h->stream);
@@ -355,7 +452,8 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
         (p.prefilter == PM_PREFILTER_GAUSSIAN && !(p.gaussian_sigma > 0.0f)) ||
         (p.precision != PM_PRECISION_FP32 && p.precision != PM_PRECISION_MIXED) ||
         p.init_mode != PM_INIT_RANDOM ||
-        (p.threads_per_line != 0 && p.threads_per_line != 32))
+        (p.threads_per_line % 32 != 0 || p.threads_per_line < 0 ||
+         p.threads_per_line > 32 * MAX_WARPS_PER_LINE))
         return PM_ERR_INVALID_ARGUMENT;
     for (int i = 0; i < n_views; ++i) {
         const pm_view &v = views[i];
@@ -429,6 +527,7 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
     PM_TRY(dalloc(&h->d_ref, npix * 4, s));
     PM_TRY(dalloc(&h->d_sum_i, npix * 4, s));
     PM_TRY(dalloc(&h->d_sum_ii, npix * 4, s));
+    PM_TRY(dalloc(&h->d_c1, npix * 4, s));
     PM_TRY(dalloc(&h->d_depth, npix * 4, s));
     PM_TRY(dalloc(&h->d_cost, npix * h->V * 4, s));
     PM_TRY(dalloc(&h->d_beta, npix * h->V * 4, s));
@@ -450,12 +549,14 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
     }
     const size_t max_pix = (size_t)max_w * max_h;
     uint8_t *d_u8 = nullptr;
-    float *d_f0 = nullptr, *d_f1 = nullptr, *d_f2 = nullptr, *d_tmp2 = nullptr;
+    float *d_f0 = nullptr, *d_f1 = nullptr, *d_f2 = nullptr;
+    double *d_row_i = nullptr, *d_row_ii = nullptr;
     PM_TRY(dalloc(&d_u8, max_pix, s));
     PM_TRY(dalloc(&d_f0, max_pix * 4, s));
     PM_TRY(dalloc(&d_f1, max_pix * 4, s));
     PM_TRY(dalloc(&d_f2, max_pix * 4, s));
-    PM_TRY(dalloc(&d_tmp2, max_pix * 4, s));
+    PM_TRY(dalloc(&d_row_i, npix * 8, s));
+    PM_TRY(dalloc(&d_row_ii, npix * 8, s));
     float taps[45];
     const int radius = filtered ? prefilter_taps(p.prefilter, p.gaussian_sigma, taps) : 0;
     si = 0;
@@ -472,8 +573,8 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
             texels = dst;
         }
         if (is_ref) {
-            PM_TRY(launch_box_moments(h->d_ref, d_f2, d_tmp2, h->d_sum_i, h->d_sum_ii, v.width,
-                                      v.height, p.half_window, s));
+            PM_TRY(launch_box_moments(h->d_ref, d_row_i, d_row_ii, h->d_sum_i, h->d_sum_ii,
+                                      h->d_c1, v.width, v.height, p.half_window, s));
             continue;
         }
         cudaArray_t arr = nullptr;
@@ -508,7 +609,8 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
     PM_TRY(cudaFreeAsync(d_f0, s));
     PM_TRY(cudaFreeAsync(d_f1, s));
     PM_TRY(cudaFreeAsync(d_f2, s));
-    PM_TRY(cudaFreeAsync(d_tmp2, s));
+    PM_TRY(cudaFreeAsync(d_row_i, s));
+    PM_TRY(cudaFreeAsync(d_row_ii, s));
 
     RefDesc &D = h->h_desc;
     std::memset(&D, 0, sizeof D);
@@ -530,6 +632,7 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
     D.ref = h->d_ref;
     D.sum_i = h->d_sum_i;
     D.sum_ii = h->d_sum_ii;
+    D.c1 = h->d_c1;
     D.depth = h->d_depth;
     D.cost = h->d_cost;
     D.beta = h->d_beta;
@@ -547,7 +650,6 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
     PM_TRY(cudaStreamSynchronize(s));
 #undef PM_TRY
     cudaEventElapsedTime(&h->stats.ms_prepare, h->ev[0], h->ev[1]);
-    h->stats.threads_per_line = 32;
     h->stats.texel_bytes = h->texel_bytes;
     *out = h;
     return PM_OK;
@@ -559,6 +661,8 @@ pm_status pm_run_async(pm_handle *h)
     pm_status st = set_device(h);
     if (st != PM_OK) return st;
     if (!h->graph) {
+        const cudaError_t et = tune_warps_per_line(h);
+        if (et != cudaSuccess) return cuda_fail(h, et, "warps-per-line tuning");
         cudaGraph_t g = nullptr;
         PM_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
         const cudaError_t e = enqueue_schedule(h);
@@ -636,7 +740,7 @@ pm_status pm_run_batch(pm_handle *const *hs, int n)
                 req.refs = d_descs;
                 req.ref_index = i;
                 req.axis = 1;
-                req.grid = (h->W * h->H + 3) / 4;
+                req.grid = (h->W * h->H + COST_BLOCK / 32 - 1) / (COST_BLOCK / 32);
                 PM_CUDA(h0, launch_window(h->win, req));
                 max_iters = std::max(max_iters, h->p.num_iterations);
             }
@@ -647,13 +751,11 @@ pm_status pm_run_batch(pm_handle *const *hs, int n)
                     std::vector<int> lines(m, 0);
                     for (int i = 0; i < m; ++i)
                         lines[i] = grp[start + i]->p.num_iterations > it ? lines_of(grp[start + i], d) : 0;
-                    // a reference whose last iteration is `it` records its view selection;
-                    // the kernel flag is per launch, so record for everyone on the global
-                    // last iteration and rely on per-reference iteration counts otherwise
+                    // every bottom-to-top sweep records; a reference's last one writes last
                     SweepArgs &a = args[(size_t)it * 4 + d];
                     fill_sweep_args(a, d_descs, lines.data(), m, d, (uint32_t)(4 * it + d),
                                     it == 0 ? 1 : 0, d == PM_DIR_BOTTOM_TO_TOP ? 1 : 0);
-                    PM_CUDA(h0, enqueue_sweep(grp[start]->win, a, s));
+                    PM_CUDA(h0, enqueue_sweep(grp[start]->win, batch_wpl(grp[start]->win, a.total_lines, h0->device), a, s));
                 }
             PM_CUDA(h0, cudaFreeAsync(d_descs, s));
         }
@@ -763,12 +865,26 @@ pm_status pm_run_sweep(pm_handle *h, int direction, uint32_t sweep_id, int num_s
     const int lines = lines_of(h, direction);
     fill_sweep_args(a, h->d_desc, &lines, 1, direction, sweep_id, num_samples, record_views ? 1 : 0);
     if (record_views && num_samples > h->p.num_samples) return PM_ERR_INVALID_ARGUMENT;
+    if (!h->wpl[orient(direction)]) {
+        // tune on scratch copies so the caller's state is untouched
+        std::vector<float> d((size_t)h->W * h->H), c((size_t)h->W * h->H * h->V);
+        PM_CUDA(h, cudaMemcpyAsync(d.data(), h->d_depth, d.size() * 4, cudaMemcpyDeviceToHost, h->stream));
+        PM_CUDA(h, cudaMemcpyAsync(c.data(), h->d_cost, c.size() * 4, cudaMemcpyDeviceToHost, h->stream));
+        PM_CUDA(h, cudaStreamSynchronize(h->stream));
+        PM_CUDA(h, tune_warps_per_line(h));
+        PM_CUDA(h, cudaMemcpyAsync(h->d_depth, d.data(), d.size() * 4, cudaMemcpyHostToDevice, h->stream));
+        PM_CUDA(h, cudaMemcpyAsync(h->d_cost, c.data(), c.size() * 4, cudaMemcpyHostToDevice, h->stream));
+    }
     PM_CUDA(h, cudaEventRecord(h->ev[2], h->stream));
-    PM_CUDA(h, enqueue_sweep(h->win, a, h->stream));
+    PM_CUDA(h, enqueue_sweep(h->win, h->wpl[orient(direction)], a, h->stream));
     PM_CUDA(h, cudaEventRecord(h->ev[3], h->stream));
     PM_CUDA(h, cudaStreamSynchronize(h->stream));
     float ms = 0.0f;
     if (cudaEventElapsedTime(&ms, h->ev[2], h->ev[3]) == cudaSuccess) h->stats.ms_sweeps = ms;
+    unsigned long long ev[2];
+    PM_CUDA(h, cudaMemcpy(ev, h->d_evals, sizeof ev, cudaMemcpyDeviceToHost));
+    h->stats.cost_evals = ev[0];
+    h->stats.cost_evals_done = ev[1];
     if (record_views) h->ran = true;
     return PM_OK;
 }
@@ -870,7 +986,7 @@ pm_status pm_eval_costs(pm_handle *h, int n, const int *xs, const int *ys, const
     req.queries = d_q;
     req.depths = d_d;
     req.out = d_o;
-    req.grid = std::min((n + 3) / 4, 65535);
+    req.grid = std::min((n + COST_BLOCK / 32 - 1) / (COST_BLOCK / 32), 65535);
     PM_CUDA(h, launch_window(h->win, req));
     PM_CUDA(h, cudaMemcpyAsync(out, d_o, sizeof(float) * n, cudaMemcpyDeviceToHost, s));
     PM_CUDA(h, cudaFreeAsync(d_q, s));

@@ -42,6 +42,7 @@ struct RefDesc {
     const float *ref;               // height*width texels
     const float *sum_i;             // box sums of the window
     const float *sum_ii;
+    const float *c1;                // S_II - S_I^2 / n (FP64 prep), clamped below 1e-5
     float *depth;                   // height*width
     float *cost;                    // height*width*n_src, pixel-major
     float *beta;                    // scratch: width*height*n_src backward messages
@@ -101,21 +102,6 @@ __device__ __forceinline__ float warp_sum(float v)
     return v;
 }
 
-// 1 - NCC from the window moments (patchMatch.cu:594-610): 2 when the source window is all
-// zero, variances below 1e-5 clamp to 0, 1 when their product is 0.
-__device__ __forceinline__ float ncc_finalize(float sj, float sjj, float sij, float si,
-                                              float sii, float n)
-{
-    if (sjj == 0.0f) return 2.0f;
-    float c1 = sii - si * si / n;
-    float c2 = sjj - sj * sj / n;
-    c1 = c1 < 0.00001f ? 0.0f : c1;
-    c2 = c2 < 0.00001f ? 0.0f : c2;
-    const float c = sqrtf(c1 * c2);
-    if (c == 0.0f) return 1.0f;
-    return 1.0f - (sij - si * sj / n) / c;
-}
-
 // HMM messages (patchMatch.cu:669-715). e = exp(-c^2 / (2 a2)); a cost of exactly 2 is
 // replaced by 2 U(0,1] by the caller.
 __device__ __forceinline__ float emission(float c, float a2) { return expf(-0.5f * c * c / a2); }
@@ -143,13 +129,24 @@ struct Window {
 };
 
 // Per-step state of one pixel's window, held by every lane for its own slots.
+//
+// The reference evaluates 1 - (S_IJ - S_I S_J / n) / sqrt(c1 c2) from raw sums
+// (patchMatch.cu:594-610), which cancels badly in FP32 for weakly textured windows. Here
+//   c1 = S_II - S_I^2 / n          comes from the FP64 preparation pass (per pixel),
+//   c2 = sum (J - mu_J)^2          is summed from source samples centred on their own mean,
+//   cov = sum (J - mu_J)(R - mu) + mu_J * sum (R - mu)
+// with mu = S_I / n the reference window mean and R the reference value the reference pairs
+// with each source sample. In exact arithmetic this equals the reference's covariance,
+// including its leading-edge misalignment (the last term is zero for aligned windows).
 template <int W>
 struct PixelWindow {
     static constexpr int NS = Window<W>::NS;
-    float rv[NS];        // reference value paired with the slot (0 when out of bounds)
+    float b[NS];         // R - mu for the slot's paired reference value (in-bounds slots)
     uint64_t inb;        // slot in bounds
     float ox, oy;        // window origin in reference pixel-centre coordinates
-    float si, sii, n;    // box sums and in-bounds count
+    float n, inv_n;      // in-bounds count
+    float c1;            // reference variance term, clamped
+    float bsum;          // sum over in-bounds slots of (R - mu)
     float scale;         // plane scale at this pixel
 };
 
@@ -157,9 +154,7 @@ struct PixelWindow {
 // column axis for the reference's misalignment (0: x, vertical sweeps; 1: y).
 template <int W>
 __device__ __forceinline__ void load_window(const RefDesc &D, int x, int y, int axis, int lane,
-                                            const float (&fdx)[Window<W>::NS],
-                                            const float (&fdy)[Window<W>::NS],
-                                            PixelWindow<W> &pw)
+                                            const float2 *slots, PixelWindow<W> &pw)
 {
     constexpr int HW = Window<W>::HW, NS = Window<W>::NS, NSAMP = Window<W>::NSAMP;
     const int Wd = D.width, Hd = D.height;
@@ -169,30 +164,48 @@ __device__ __forceinline__ void load_window(const RefDesc &D, int x, int y, int 
         if (axis == 0) lead_x = x0 < 0 ? -x0 : 0;
         else lead_y = y0 < 0 ? -y0 : 0;
     }
+    const int cx0 = max(x0, 0), cx1 = min(x + HW, Wd - 1);
+    const int cy0 = max(y0, 0), cy1 = min(y + HW, Hd - 1);
+    pw.n = (float)((cx1 - cx0 + 1) * (cy1 - cy0 + 1));
+    pw.inv_n = 1.0f / pw.n;
+    const size_t pix = (size_t)y * Wd + x;
+    const float mu = __ldg(D.sum_i + pix) / pw.n;
+    pw.c1 = __ldg(D.c1 + pix);
     uint64_t inb = 0;
+    float bs = 0.0f;
 #pragma unroll
     for (int i = 0; i < NS; ++i) {
         const int k = lane + 32 * i;
-        const int xx = x0 + (int)fdx[i], yy = y0 + (int)fdy[i];
+        const float2 o = slots[32 * i + lane];
+        const int xx = x0 + (int)o.x, yy = y0 + (int)o.y;
         const bool in = (k < NSAMP) && xx >= 0 && xx < Wd && yy >= 0 && yy < Hd;
         float r = 0.0f;
         if (in) {
             const int rx = xx - lead_x, ry = yy - lead_y;
             if (rx >= 0 && ry >= 0) r = __ldg(D.ref + (size_t)ry * Wd + rx);
             inb |= (uint64_t)1 << i;
+            r -= mu;
+            bs += r;
         }
-        pw.rv[i] = r;
+        pw.b[i] = r;
     }
     pw.inb = inb;
+    pw.bsum = warp_sum(bs);
     pw.ox = (float)x0 + 0.5f;
     pw.oy = (float)y0 + 0.5f;
-    const int cx0 = max(x0, 0), cx1 = min(x + HW, Wd - 1);
-    const int cy0 = max(y0, 0), cy1 = min(y + HW, Hd - 1);
-    pw.n = (float)((cx1 - cx0 + 1) * (cy1 - cy0 + 1));
-    const size_t pix = (size_t)y * Wd + x;
-    pw.si = __ldg(D.sum_i + pix);
-    pw.sii = __ldg(D.sum_ii + pix);
     pw.scale = D.nx * (D.ik00 * ((float)x + 0.5f) + D.ik02) + D.nz;
+}
+
+// 1 - NCC (patchMatch.cu:594-610): 2 when every source sample is zero, variances below 1e-5
+// clamp to 0, 1 when their product is 0.
+__device__ __forceinline__ float ncc_finalize(float sj, float c2, float x, float c1, float mu_j,
+                                              float bsum)
+{
+    if (sj == 0.0f) return 2.0f;
+    c2 = c2 < 0.00001f ? 0.0f : c2;
+    const float c = sqrtf(c1 * c2);
+    if (c == 0.0f) return 1.0f;
+    return 1.0f - fmaf(mu_j, bsum, x) / c;
 }
 
 // Plane-induced homography of (view, depth) applied at the window origin:
@@ -224,13 +237,21 @@ __device__ __forceinline__ WarpSetup warp_setup(const RefDesc &D, int view, floa
     return w;
 }
 
+__device__ __forceinline__ float warp_sample(const WarpSetup &A, cudaTextureObject_t tex, float sw,
+                                             float sh, float dx, float dy)
+{
+    const float px = fmaf(A.c0x, dx, fmaf(A.c1x, dy, A.bx));
+    const float py = fmaf(A.c0y, dx, fmaf(A.c1y, dy, A.by));
+    const float pz = fmaf(A.c0z, dx, fmaf(A.c1z, dy, A.bz));
+    const float r = __fdividef(1.0f, pz);
+    return sample_source(tex, px * r, py * r, sw, sh);
+}
+
 // Two windowed NCC evaluations (views va/vb at depths da/db) for one pixel; every lane
-// returns both results. Interleaving two evaluations doubles the independent fetches per
-// lane.
+// returns both results. The samples stay in registers for the centred second pass.
 template <int W>
 __device__ __forceinline__ void eval_pair(const RefDesc &D, const PixelWindow<W> &pw,
-                                          const float (&fdx)[Window<W>::NS],
-                                          const float (&fdy)[Window<W>::NS], int va, float da,
+                                          const float2 *slots, int lane, int va, float da,
                                           int vb, float db, float &out_a, float &out_b)
 {
     constexpr int NS = Window<W>::NS;
@@ -238,42 +259,78 @@ __device__ __forceinline__ void eval_pair(const RefDesc &D, const PixelWindow<W>
     const WarpSetup B = warp_setup(D, vb, db, pw.scale, pw.ox, pw.oy);
     const cudaTextureObject_t ta = D.tex[va], tb = D.tex[vb];
     const float swa = D.src_w[va], sha = D.src_h[va], swb = D.src_w[vb], shb = D.src_h[vb];
-    float ja = 0.f, jja = 0.f, ija = 0.f, jb = 0.f, jjb = 0.f, ijb = 0.f;
+    float sa[NS], sb[NS];
+    float ja = 0.f, jb = 0.f;
+#pragma unroll
+    for (int i = 0; i < NS; ++i) {
+        sa[i] = 0.f;
+        sb[i] = 0.f;
+        if (pw.inb & ((uint64_t)1 << i)) {
+            const float2 o = slots[32 * i + lane];
+            sa[i] = warp_sample(A, ta, swa, sha, o.x, o.y);
+            sb[i] = warp_sample(B, tb, swb, shb, o.x, o.y);
+            ja += sa[i];
+            jb += sb[i];
+        }
+    }
+    ja = warp_sum(ja);
+    jb = warp_sum(jb);
+    const float ma = ja * pw.inv_n, mb = jb * pw.inv_n;
+    float qa = 0.f, xa = 0.f, qb = 0.f, xb = 0.f;
 #pragma unroll
     for (int i = 0; i < NS; ++i) {
         if (pw.inb & ((uint64_t)1 << i)) {
-            const float dx = fdx[i], dy = fdy[i];
-            const float pxa = fmaf(A.c0x, dx, fmaf(A.c1x, dy, A.bx));
-            const float pya = fmaf(A.c0y, dx, fmaf(A.c1y, dy, A.by));
-            const float pza = fmaf(A.c0z, dx, fmaf(A.c1z, dy, A.bz));
-            const float pxb = fmaf(B.c0x, dx, fmaf(B.c1x, dy, B.bx));
-            const float pyb = fmaf(B.c0y, dx, fmaf(B.c1y, dy, B.by));
-            const float pzb = fmaf(B.c0z, dx, fmaf(B.c1z, dy, B.bz));
-            const float ra = __fdividef(1.0f, pza), rb = __fdividef(1.0f, pzb);
-            const float sa = sample_source(ta, pxa * ra, pya * ra, swa, sha);
-            const float sb = sample_source(tb, pxb * rb, pyb * rb, swb, shb);
-            const float r = pw.rv[i];
-            ja += sa; jja = fmaf(sa, sa, jja); ija = fmaf(r, sa, ija);
-            jb += sb; jjb = fmaf(sb, sb, jjb); ijb = fmaf(r, sb, ijb);
+            const float ea = sa[i] - ma, eb = sb[i] - mb;
+            qa = fmaf(ea, ea, qa); xa = fmaf(ea, pw.b[i], xa);
+            qb = fmaf(eb, eb, qb); xb = fmaf(eb, pw.b[i], xb);
         }
     }
-    ja = warp_sum(ja); jja = warp_sum(jja); ija = warp_sum(ija);
-    jb = warp_sum(jb); jjb = warp_sum(jjb); ijb = warp_sum(ijb);
-    out_a = ncc_finalize(ja, jja, ija, pw.si, pw.sii, pw.n);
-    out_b = ncc_finalize(jb, jjb, ijb, pw.si, pw.sii, pw.n);
+    qa = warp_sum(qa); xa = warp_sum(xa);
+    qb = warp_sum(qb); xb = warp_sum(xb);
+    out_a = ncc_finalize(ja, qa, xa, pw.c1, ma, pw.bsum);
+    out_b = ncc_finalize(jb, qb, xb, pw.c1, mb, pw.bsum);
 }
 
-// Per-lane slot offsets (dx, dy) of the window.
 template <int W>
-__device__ __forceinline__ void slot_offsets(int lane, float (&fdx)[Window<W>::NS],
-                                             float (&fdy)[Window<W>::NS])
+__device__ __forceinline__ float eval_one(const RefDesc &D, const PixelWindow<W> &pw,
+                                          const float2 *slots, int lane, int v, float d)
 {
+    constexpr int NS = Window<W>::NS;
+    const WarpSetup A = warp_setup(D, v, d, pw.scale, pw.ox, pw.oy);
+    const cudaTextureObject_t ta = D.tex[v];
+    const float sw = D.src_w[v], sh = D.src_h[v];
+    float sa[NS];
+    float ja = 0.f;
 #pragma unroll
-    for (int i = 0; i < Window<W>::NS; ++i) {
-        const int k = lane + 32 * i;
-        fdx[i] = (float)(k % W);
-        fdy[i] = (float)(k / W);
+    for (int i = 0; i < NS; ++i) {
+        sa[i] = 0.f;
+        if (pw.inb & ((uint64_t)1 << i)) {
+            const float2 o = slots[32 * i + lane];
+            sa[i] = warp_sample(A, ta, sw, sh, o.x, o.y);
+            ja += sa[i];
+        }
     }
+    ja = warp_sum(ja);
+    const float ma = ja * pw.inv_n;
+    float qa = 0.f, xa = 0.f;
+#pragma unroll
+    for (int i = 0; i < NS; ++i) {
+        if (pw.inb & ((uint64_t)1 << i)) {
+            const float ea = sa[i] - ma;
+            qa = fmaf(ea, ea, qa); xa = fmaf(ea, pw.b[i], xa);
+        }
+    }
+    qa = warp_sum(qa); xa = warp_sum(xa);
+    return ncc_finalize(ja, qa, xa, pw.c1, ma, pw.bsum);
+}
+
+// Window offsets (dx, dy) of every lane's slots: table[32 * i + lane] for slot i, filled
+// cooperatively by a CTA (synchronise before use).
+template <int W>
+__device__ __forceinline__ void fill_slot_table(float2 *table)
+{
+    for (int k = threadIdx.x; k < 32 * Window<W>::NS; k += blockDim.x)
+        table[k] = make_float2((float)(k % W), (float)(k / W));
 }
 
 }  // namespace pm

@@ -8,12 +8,14 @@
 
 namespace pm {
 
-enum class LaunchKind { Sweep, Costs, Eval };
+enum class LaunchKind { Sweep, Costs, Eval, SweepOccupancy };
 
 struct LaunchReq {
     LaunchKind kind;
     cudaStream_t stream;
     int grid;
+    int block;                 // Sweep: 32 * warps per line
+    int *occupancy;            // SweepOccupancy: active CTAs per SM for `block`
     // Sweep
     const SweepArgs *sweep;
     // Costs / Eval
@@ -46,8 +48,8 @@ cudaError_t launch_u8_to_float(const uint8_t *in, int in_pitch, float *out, int 
                                cudaStream_t s);
 cudaError_t launch_filter(const float *in, float *tmp, float *out, int w, int h, int radius,
                           const float *weights, cudaStream_t s);
-cudaError_t launch_box_moments(const float *img, float *row_i, float *row_ii, float *sum_i,
-                               float *sum_ii, int w, int h, int hw, cudaStream_t s);
+cudaError_t launch_box_moments(const float *img, double *row_i, double *row_ii, float *sum_i,
+                               float *sum_ii, float *c1, int w, int h, int hw, cudaStream_t s);
 cudaError_t launch_float_to_half(const float *in, void *out, int n, cudaStream_t s);
 cudaError_t launch_init_depth(const RefDesc *refs, int r, int npix, cudaStream_t s);
 cudaError_t launch_sample(const RefDesc *refs, int r, int view, int n, const float *xs,

@@ -2,7 +2,7 @@
 //
 //  u8 -> float texels (cudaReadModeNormalizedFloat of patchMatch.cu:27-28 made explicit),
 //  separable prefilter (GaussianBlurCUDA.cu:39-70), reference-window box moments
-//  (array2d_refImg.cu:11-67), FP16 texel conversion, random initial depth
+//  (array2d_refImg.cu:11-67, summed in double here), FP16 texel conversion, random initial depth
 //  (array2d_wrapper.cu:3-20), source sampling queries, the layered transpose
 //  (cudaTranspose.h:9-46) and raw Philox output.
 #include <cuda_fp16.h>
@@ -41,15 +41,16 @@ __global__ void filter_pass_kernel(const float *__restrict__ in, float *__restri
     out[(size_t)y * w + x] = s;
 }
 
-__global__ void box_rows_kernel(const float *__restrict__ img, float *__restrict__ ri,
-                                float *__restrict__ rii, int w, int h, int hw)
+// Row pass of the window box sums in double precision.
+__global__ void box_rows_kernel(const float *__restrict__ img, double *__restrict__ ri,
+                                double *__restrict__ rii, int w, int h, int hw)
 {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= w || y >= h) return;
-    float a = 0.0f, b = 0.0f;
+    double a = 0.0, b = 0.0;
     for (int k = -hw; k <= hw; ++k) {
         const int xx = x + k;
-        const float v = (xx >= 0 && xx < w) ? img[(size_t)y * w + xx] : 0.0f;
+        const double v = (xx >= 0 && xx < w) ? (double)img[(size_t)y * w + xx] : 0.0;
         a += v;
         b += v * v;
     }
@@ -57,21 +58,27 @@ __global__ void box_rows_kernel(const float *__restrict__ img, float *__restrict
     rii[(size_t)y * w + x] = b;
 }
 
-__global__ void box_cols_kernel(const float *__restrict__ ri, const float *__restrict__ rii,
-                                float *__restrict__ si, float *__restrict__ sii, int w, int h,
-                                int hw)
+// Column pass; also the reference variance term c1 = S_II - S_I^2 / n over the n in-bounds
+// window pixels, clamped to 0 below 1e-5 like patchMatch.cu:597-599.
+__global__ void box_cols_kernel(const double *__restrict__ ri, const double *__restrict__ rii,
+                                float *__restrict__ si, float *__restrict__ sii,
+                                float *__restrict__ c1, int w, int h, int hw)
 {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= w || y >= h) return;
-    float a = 0.0f, b = 0.0f;
+    double a = 0.0, b = 0.0;
     for (int k = -hw; k <= hw; ++k) {
         const int yy = y + k;
         if (yy < 0 || yy >= h) continue;
         a += ri[(size_t)yy * w + x];
         b += rii[(size_t)yy * w + x];
     }
-    si[(size_t)y * w + x] = a;
-    sii[(size_t)y * w + x] = b;
+    const int nx = min(x + hw, w - 1) - max(x - hw, 0) + 1;
+    const int ny = min(y + hw, h - 1) - max(y - hw, 0) + 1;
+    const double v = b - a * a / (double)(nx * ny);
+    si[(size_t)y * w + x] = (float)a;
+    sii[(size_t)y * w + x] = (float)b;
+    c1[(size_t)y * w + x] = v < 0.00001 ? 0.0f : (float)v;
 }
 
 __global__ void float_to_half_kernel(const float *__restrict__ in, __half *__restrict__ out, int n)
@@ -149,12 +156,12 @@ cudaError_t launch_filter(const float *in, float *tmp, float *out, int w, int h,
     return cudaGetLastError();
 }
 
-cudaError_t launch_box_moments(const float *img, float *row_i, float *row_ii, float *sum_i,
-                               float *sum_ii, int w, int h, int hw, cudaStream_t s)
+cudaError_t launch_box_moments(const float *img, double *row_i, double *row_ii, float *sum_i,
+                               float *sum_ii, float *c1, int w, int h, int hw, cudaStream_t s)
 {
     const dim3 b(32, 8);
     box_rows_kernel<<<grid2d(w, h, b), b, 0, s>>>(img, row_i, row_ii, w, h, hw);
-    box_cols_kernel<<<grid2d(w, h, b), b, 0, s>>>(row_i, row_ii, sum_i, sum_ii, w, h, hw);
+    box_cols_kernel<<<grid2d(w, h, b), b, 0, s>>>(row_i, row_ii, sum_i, sum_ii, c1, w, h, hw);
     return cudaGetLastError();
 }
 
