@@ -43,7 +43,27 @@ def parse_args():
     ap.add_argument("--precision", type=int, default=0, help="0 = FP32, 1 = FP16 texels (mixed)")
     ap.add_argument("--cpu-seconds", type=float, default=8.0, help="CPU baseline sample budget")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", type=int, default=None, metavar="DIR",
+                    help="run only the initial state and one sweep in direction DIR (for ncu)")
+    ap.add_argument("--threads-per-line", type=int, default=0)
     return ap.parse_args()
+
+
+def run_profile(args):
+    """Initial depth and costs, then one sweep: the launches an ncu capture looks at."""
+    from patchmatch_cuda_gb300 import Engine, scene
+    wl = scene.WORKLOADS[args.workload]
+    sv = scene.make_views(wl)
+    eng = Engine(sv.images, sv.ref_id, wl.params(precision=args.precision,
+                                                  threads_per_line=args.threads_per_line))
+    eng.init_depth()
+    eng.compute_costs(1)
+    eng.run_sweep(args.profile, 4 + args.profile, wl.num_samples)
+    st = eng.stats()
+    print(json.dumps({"sweep_ms": st.ms_sweeps, "cost_evals": st.cost_evals,
+                      "threads_per_line": st.threads_per_line}))
+    eng.close()
+    return 0
 
 
 class ClockSampler:
@@ -188,7 +208,7 @@ def run_reference(args):
     orc = pm_oracle.from_images(sv.images, sv.ref_id, _plain_params(wl), fp32=True)
     depth0 = orc.init_depth()
     S = wl.num_samples
-    lines = 16
+    lines = 256
     cost0 = _sample_costs(orc, depth0, lines)
     times, evals = [], []
     for step in range(args.warmup + args.steps):
@@ -374,6 +394,8 @@ def run_ours(args):
 
 def main():
     args = parse_args()
+    if args.profile is not None:
+        return run_profile(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -310,6 +310,7 @@ cudaError_t tune_warps_per_line(pm_handle *h)
     if (h->wpl[0] && h->wpl[1]) return cudaSuccess;
     if (h->p.threads_per_line) {
         h->wpl[0] = h->wpl[1] = h->p.threads_per_line / 32;
+        h->stats.threads_per_line = h->p.threads_per_line;
         return cudaSuccess;
     }
     cudaError_t e = cudaSuccess;

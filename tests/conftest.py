@@ -23,3 +23,20 @@ def oracle_lib():
 def engine_lib():
     from patchmatch_cuda_gb300 import _native
     return _native.load_engine()
+
+
+@pytest.fixture(scope="session")
+def parity_log():
+    """Records measured parity figures; written as JSON to $PM_PARITY_LOG when set."""
+    import json
+    import os
+    records = {}
+
+    def log(name, **values):
+        records[name] = values
+
+    yield log
+    path = os.environ.get("PM_PARITY_LOG")
+    if path and records:
+        with open(path, "w") as f:
+            json.dump(records, f, indent=1, sort_keys=True)
