@@ -61,6 +61,19 @@ typedef enum pm_precision {
     PM_PRECISION_MIXED = 1      /* FP16 texels, shifted window moments, FP64 window origin    */
 } pm_precision;
 
+typedef enum pm_sampler {
+    PM_SAMPLER_EXACT = 0,       /* 4-texel gather, exact FP32 bilinear weights              */
+    PM_SAMPLER_HARDWARE = 1     /* texture-unit bilinear filtering, 8-bit fixed-point weights
+                                   (what the reference's tex2DLayered fetch does)           */
+} pm_sampler;
+
+typedef enum pm_texel_format {
+    PM_TEXELS_AUTO = 0,         /* chosen from precision and prefilter                        */
+    PM_TEXELS_U8 = 1,           /* unfiltered images only                                     */
+    PM_TEXELS_F16 = 2,
+    PM_TEXELS_F32 = 4
+} pm_texel_format;
+
 typedef enum pm_init_mode {
     PM_INIT_RANDOM = 0          /* uniform depth in [near, far) (array2d_wrapper.cu:3-20)      */
 } pm_init_mode;
@@ -101,6 +114,8 @@ typedef struct pm_params {
                                       misalignment (patchMatch.cu:546); 0: aligned windows   */
     int gpu_id;                    /* gpuId: -1 = current device (main.cpp:56-59)            */
     int block_dim_x, block_dim_y;  /* accepted for signature parity, unused                  */
+    int sampler;                   /* pm_sampler                                             */
+    int texel_format;              /* pm_texel_format                                        */
 } pm_params;
 
 typedef struct pm_handle pm_handle;

@@ -22,6 +22,8 @@ STATUS_NAMES = {
 
 PREFILTER_NONE, PREFILTER_BOX, PREFILTER_GAUSSIAN = 0, 1, 2
 PRECISION_FP32, PRECISION_MIXED = 0, 1
+SAMPLER_EXACT, SAMPLER_HARDWARE = 0, 1
+TEXELS_AUTO, TEXELS_U8, TEXELS_F16, TEXELS_F32 = 0, 1, 2, 4
 DIR_LEFT_TO_RIGHT, DIR_TOP_TO_BOTTOM, DIR_RIGHT_TO_LEFT, DIR_BOTTOM_TO_TOP = 0, 1, 2, 3
 
 # Every symbol include/patchmatch_gb300.h declares.
@@ -50,6 +52,7 @@ class PmParams(C.Structure):
         ("orientation_z", C.c_float), ("seed", C.c_uint64), ("precision", C.c_int),
         ("init_mode", C.c_int), ("threads_per_line", C.c_int), ("quirks", C.c_int),
         ("gpu_id", C.c_int), ("block_dim_x", C.c_int), ("block_dim_y", C.c_int),
+        ("sampler", C.c_int), ("texel_format", C.c_int),
     ]
 
 

@@ -453,6 +453,10 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
         (p.prefilter == PM_PREFILTER_GAUSSIAN && !(p.gaussian_sigma > 0.0f)) ||
         (p.precision != PM_PRECISION_FP32 && p.precision != PM_PRECISION_MIXED) ||
         p.init_mode != PM_INIT_RANDOM ||
+        (p.sampler != PM_SAMPLER_EXACT && p.sampler != PM_SAMPLER_HARDWARE) ||
+        (p.texel_format != PM_TEXELS_AUTO && p.texel_format != PM_TEXELS_U8 &&
+         p.texel_format != PM_TEXELS_F16 && p.texel_format != PM_TEXELS_F32) ||
+        (p.texel_format == PM_TEXELS_U8 && p.prefilter != PM_PREFILTER_NONE) ||
         (p.threads_per_line % 32 != 0 || p.threads_per_line < 0 ||
          p.threads_per_line > 32 * MAX_WARPS_PER_LINE))
         return PM_ERR_INVALID_ARGUMENT;
@@ -481,7 +485,8 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
     h->V = n_views - 1;
     h->win = 2 * p.half_window + 1;
     const bool filtered = p.prefilter != PM_PREFILTER_NONE;
-    h->texel_bytes = p.precision == PM_PRECISION_FP32 ? (filtered ? 4 : 1) : (filtered ? 2 : 1);
+    h->texel_bytes = p.texel_format != PM_TEXELS_AUTO ? p.texel_format
+                     : p.precision == PM_PRECISION_FP32 ? (filtered ? 4 : 1) : (filtered ? 2 : 1);
 
     // camera setup
     double kr[9], kr_inv[9];
@@ -600,7 +605,7 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
         cudaTextureDesc td{};
         td.addressMode[0] = cudaAddressModeBorder;
         td.addressMode[1] = cudaAddressModeBorder;
-        td.filterMode = cudaFilterModePoint;
+        td.filterMode = p.sampler == PM_SAMPLER_HARDWARE ? cudaFilterModeLinear : cudaFilterModePoint;
         td.readMode = h->texel_bytes == 1 ? cudaReadModeNormalizedFloat : cudaReadModeElementType;
         td.normalizedCoords = 0;
         PM_TRY(cudaCreateTextureObject(&h->tex[si], &rd, &td, nullptr));
@@ -628,6 +633,7 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
     D.ik00 = (float)kr_inv[0];
     D.ik02 = (float)kr_inv[2];
     D.quirks = p.quirks ? 1 : 0;
+    D.hw_filter = p.sampler == PM_SAMPLER_HARDWARE ? 1 : 0;
     D.batch_id = 0;
     D.seed = p.seed;
     D.ref = h->d_ref;

@@ -37,6 +37,7 @@ struct RefDesc {
     float u_emit;                   // exp(-0.83^2 / (2 a2))
     float nx, nz, ik00, ik02;       // plane scale s = nx (ik00 (x+1/2) + ik02) + nz
     int quirks;
+    int hw_filter;                  // textures filter bilinearly in hardware
     uint32_t batch_id;
     uint64_t seed;
     const float *ref;               // height*width texels
@@ -93,6 +94,13 @@ __device__ __forceinline__ float sample_source(cudaTextureObject_t tex, float xs
     const float top = fmaf(ax, g.z - g.w, g.w);
     const float bot = fmaf(ax, g.y - g.x, g.x);
     return fmaf(ay, bot - top, top);
+}
+
+// Texture-unit bilinear filtering at source coordinate (xs, ys) (texel i at i): the fetch of
+// patchMatch.cu:543 itself, with the hardware's fixed-point weights.
+__device__ __forceinline__ float sample_source_hw(cudaTextureObject_t tex, float xs, float ys)
+{
+    return tex2D<float>(tex, xs + 0.5f, ys + 0.5f);
 }
 
 __device__ __forceinline__ float warp_sum(float v)
@@ -237,12 +245,19 @@ __device__ __forceinline__ WarpSetup warp_setup(const RefDesc &D, int view, floa
     return w;
 }
 
+template <bool HW>
 __device__ __forceinline__ float warp_sample(const WarpSetup &A, cudaTextureObject_t tex, float sw,
                                              float sh, float dx, float dy)
 {
     const float px = fmaf(A.c0x, dx, fmaf(A.c1x, dy, A.bx));
     const float py = fmaf(A.c0y, dx, fmaf(A.c1y, dy, A.by));
-    const float pz = fmaf(A.c0z, dx, fmaf(A.c1z, dy, A.bz));
+    float pz = fmaf(A.c0z, dx, fmaf(A.c1z, dy, A.bz));
+    if (HW) {
+        // keep the coordinate finite on the source camera's principal plane (border -> 0)
+        pz = fabsf(pz) < 1e-20f ? 1e-20f : pz;
+        const float r = __fdividef(1.0f, pz);
+        return sample_source_hw(tex, px * r, py * r);
+    }
     const float r = __fdividef(1.0f, pz);
     return sample_source(tex, px * r, py * r, sw, sh);
 }
@@ -261,16 +276,31 @@ __device__ __forceinline__ void eval_pair(const RefDesc &D, const PixelWindow<W>
     const float swa = D.src_w[va], sha = D.src_h[va], swb = D.src_w[vb], shb = D.src_h[vb];
     float sa[NS], sb[NS];
     float ja = 0.f, jb = 0.f;
+    if (D.hw_filter) {
 #pragma unroll
-    for (int i = 0; i < NS; ++i) {
-        sa[i] = 0.f;
-        sb[i] = 0.f;
-        if (pw.inb & ((uint64_t)1 << i)) {
-            const float2 o = slots[32 * i + lane];
-            sa[i] = warp_sample(A, ta, swa, sha, o.x, o.y);
-            sb[i] = warp_sample(B, tb, swb, shb, o.x, o.y);
-            ja += sa[i];
-            jb += sb[i];
+        for (int i = 0; i < NS; ++i) {
+            sa[i] = 0.f;
+            sb[i] = 0.f;
+            if (pw.inb & ((uint64_t)1 << i)) {
+                const float2 o = slots[32 * i + lane];
+                sa[i] = warp_sample<true>(A, ta, swa, sha, o.x, o.y);
+                sb[i] = warp_sample<true>(B, tb, swb, shb, o.x, o.y);
+                ja += sa[i];
+                jb += sb[i];
+            }
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < NS; ++i) {
+            sa[i] = 0.f;
+            sb[i] = 0.f;
+            if (pw.inb & ((uint64_t)1 << i)) {
+                const float2 o = slots[32 * i + lane];
+                sa[i] = warp_sample<false>(A, ta, swa, sha, o.x, o.y);
+                sb[i] = warp_sample<false>(B, tb, swb, shb, o.x, o.y);
+                ja += sa[i];
+                jb += sb[i];
+            }
         }
     }
     ja = warp_sum(ja);
@@ -301,13 +331,25 @@ __device__ __forceinline__ float eval_one(const RefDesc &D, const PixelWindow<W>
     const float sw = D.src_w[v], sh = D.src_h[v];
     float sa[NS];
     float ja = 0.f;
+    if (D.hw_filter) {
 #pragma unroll
-    for (int i = 0; i < NS; ++i) {
-        sa[i] = 0.f;
-        if (pw.inb & ((uint64_t)1 << i)) {
-            const float2 o = slots[32 * i + lane];
-            sa[i] = warp_sample(A, ta, sw, sh, o.x, o.y);
-            ja += sa[i];
+        for (int i = 0; i < NS; ++i) {
+            sa[i] = 0.f;
+            if (pw.inb & ((uint64_t)1 << i)) {
+                const float2 o = slots[32 * i + lane];
+                sa[i] = warp_sample<true>(A, ta, sw, sh, o.x, o.y);
+                ja += sa[i];
+            }
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < NS; ++i) {
+            sa[i] = 0.f;
+            if (pw.inb & ((uint64_t)1 << i)) {
+                const float2 o = slots[32 * i + lane];
+                sa[i] = warp_sample<false>(A, ta, sw, sh, o.x, o.y);
+                ja += sa[i];
+            }
         }
     }
     ja = warp_sum(ja);

@@ -102,7 +102,9 @@ __global__ void sample_kernel(const RefDesc *refs, int r, int view, int n,
 {
     const RefDesc &D = refs[r];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) out[i] = sample_source(D.tex[view], xs[i], ys[i], D.src_w[view], D.src_h[view]);
+    if (i < n)
+        out[i] = D.hw_filter ? sample_source_hw(D.tex[view], xs[i], ys[i])
+                             : sample_source(D.tex[view], xs[i], ys[i], D.src_w[view], D.src_h[view]);
 }
 
 // 32x32 shared tile with one column of padding against bank conflicts; blockIdx.z = layer.
