@@ -10,9 +10,14 @@
  *    (array2d_psng.cu:3-17). Here every draw is one Philox4x32-10 output keyed by
  *    (pixel, sweep, purpose, sub-index); the uniform is ((x >> 8) + 1) * 2^-24 in (0, 1],
  *    the same interval curand_uniform returns.
- *  - Bilinear source sampling uses exact weights, texel i at coordinate i, zero border:
- *    the documented semantics of the reference's tex2DLayered(u/z + 0.5, v/z + 0.5)
- *    fetch (patchMatch.cu:543) without the hardware's 8-bit weight quantisation.
+ *  - Bilinear source sampling, texel i at coordinate i, zero border (the reference's
+ *    tex2DLayered(u/z + 0.5, v/z + 0.5) fetch, patchMatch.cu:543), either with exact
+ *    weights or with the texture unit's fixed-point weights (sampler 1).
+ *  - Message storage: the reference keeps emissions in float and builds with
+ *    --use_fast_math (cmakelists_32bit.txt:11), so an emission below FLT_MIN becomes 0 and
+ *    so do messages and posteriors that fall below FLT_MIN. This restatement rounds the
+ *    emission to float and flushes those values to zero as well; where every view's
+ *    posterior is then zero the CDF is 0/0 and no view is sampled.
  *  - A view sample whose CDF search finds no view (only possible when the posterior
  *    CDF is NaN) is skipped; the reference then indexes layer -1 (undefined). If no
  *    sample of a pixel finds a view the current depth is kept.
@@ -262,7 +267,11 @@ static inline real texel(const float *img, int w, int h, int x, int y)
     return (x >= 0 && x < w && y >= 0 && y < h) ? (real)img[(size_t)y * w + x] : (real)0;
 }
 
-static inline real sample_bilinear(const float *img, int w, int h, real xs, real ys)
+/* Texture-unit weight: a fraction rounded half-up to a multiple of 1/256 (measured on the
+ * GB300's texture units; the CUDA programming guide documents 8 fractional bits). */
+static inline real q8(real f) { return R_FLOOR(f * (real)256 + (real)0.5) / (real)256; }
+
+static inline real sample_bilinear(const float *img, int w, int h, real xs, real ys, int hw)
 {
     if (!(xs > (real)-1 && xs < (real)w && ys > (real)-1 && ys < (real)h)) return 0;
     real fx = R_FLOOR(xs), fy = R_FLOOR(ys);
@@ -270,8 +279,20 @@ static inline real sample_bilinear(const float *img, int w, int h, real xs, real
     real ax = xs - fx, ay = ys - fy;
     real t00 = texel(img, w, h, x0, y0), t10 = texel(img, w, h, x0 + 1, y0);
     real t01 = texel(img, w, h, x0, y0 + 1), t11 = texel(img, w, h, x0 + 1, y0 + 1);
+    if (hw) {
+        const real a = q8(ax), b = q8(ay), ab = q8(a * b);
+        return t00 * ((real)1 - a - b + ab) + t10 * (a - ab) + t01 * (b - ab) + t11 * ab;
+    }
     return ((real)1 - ax) * ((real)1 - ay) * t00 + ax * ((real)1 - ay) * t10 +
            ((real)1 - ax) * ay * t01 + ax * ay * t11;
+}
+
+void pmo_sample(const pmo_problem *p, int view, int n, const float *xs, const float *ys,
+                double *out)
+{
+    for (int i = 0; i < n; ++i)
+        out[i] = (double)sample_bilinear(p->src[view], p->src_width[view], p->src_height[view],
+                                         (real)xs[i], (real)ys[i], p->sampler);
 }
 
 /* Plane scale s = n^T K^-1 (x + 1/2, y + 1/2, 1): patchMatch.cu:798-800, :876-883 with
@@ -319,7 +340,7 @@ static real ncc_eval(const pmo_problem *p, const double *sum_i, const double *su
             real u = t[0] * px + t[1] * py + t[2];
             real v = t[3] * px + t[4] * py + t[5];
             real z = t[6] * px + t[7] * py + t[8];
-            real jv = sample_bilinear(src, sw, sh, u / z, v / z);
+            real jv = sample_bilinear(src, sw, sh, u / z, v / z, p->sampler);
             int rx = axis == 0 ? xx - lead : xx;
             int ry = axis == 0 ? yy : yy - lead;
             real iv = texel(p->ref, W, H, rx, ry);
@@ -373,20 +394,27 @@ static inline real uniform_emission(real a2)
     return R_EXP((real)-0.5 * UNIFORM_EMISSION_COST * UNIFORM_EMISSION_COST / a2);
 }
 
-static inline real emission(real c, real a2) { return R_EXP((real)-0.5 * c * c / a2); }
+/* Values below the smallest normal float flush to zero (the reference's float storage
+ * under --use_fast_math). */
+static inline real ftz(real x) { return (x < (real)1.17549435e-38f && x > (real)-1.17549435e-38f) ? (real)0 : x; }
+
+static inline real emission(real c, real a2)
+{
+    return ftz((real)(float)R_EXP((real)-0.5 * c * c / a2));
+}
 
 static inline real msg_backward(real m, real e, real u)
 {
     real zn0 = m * e * FIX_STATE_PROB + ((real)1 - m) * u * CHANGE_STATE_PROB;
     real zn1 = m * e * CHANGE_STATE_PROB + ((real)1 - m) * u * FIX_STATE_PROB;
-    return zn0 / (zn0 + zn1);
+    return ftz(zn0 / (zn0 + zn1));
 }
 
 static inline real msg_forward(real m, real e, real u)
 {
     real zn0 = (m * FIX_STATE_PROB + ((real)1 - m) * CHANGE_STATE_PROB) * e;
     real zn1 = (m * CHANGE_STATE_PROB + ((real)1 - m) * FIX_STATE_PROB) * u;
-    return zn0 / (zn0 + zn1);
+    return ftz(zn0 / (zn0 + zn1));
 }
 
 double pmo_msg_forward(double msg, double cost, double u_if_two, float sp_alpha)
@@ -535,7 +563,7 @@ long long pmo_sweep(const pmo_problem *p, const double *sum_i, const double *sum
                     real b = beta_all[(size_t)k * V + v];
                     real zn0 = a * b;
                     real zn1 = ((real)1 - a) * ((real)1 - b);
-                    cdf[v] = zn0 / (zn0 + zn1);
+                    cdf[v] = ftz(zn0 / (zn0 + zn1));
                 }
                 for (int v = 1; v < V; ++v) cdf[v] += cdf[v - 1];
                 for (int v = 0; v < V; ++v) cdf[v] /= cdf[V - 1];

@@ -59,6 +59,9 @@ typedef struct pmo_problem {
     uint32_t batch_id;              /* fourth Philox counter word                          */
     int quirks;                     /* nonzero: keep the reference's ref/source window
                                        misalignment at the leading edge (:546)            */
+    int sampler;                    /* 0: exact bilinear weights; 1: texture-unit weights
+                                       (fractions rounded half-up to 1/256, cross term
+                                       alpha*beta rounded likewise)                       */
 } pmo_problem;
 
 void pmo_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
@@ -73,6 +76,9 @@ int pmo_prefilter(const float *in, int width, int height, int mode, float sigma,
 void pmo_box_moments(const float *img, int width, int height, int half_window,
                      double *sum_i, double *sum_ii);
 
+/* Source fetch at texel coordinates (texel i at i), patchMatch.cu:543. */
+void pmo_sample(const pmo_problem *p, int view, int n, const float *xs, const float *ys,
+                double *out);
 double pmo_ncc(const pmo_problem *p, const double *sum_i, const double *sum_ii,
                int x, int y, int view, double depth, int axis);
 void pmo_ncc_batch(const pmo_problem *p, const double *sum_i, const double *sum_ii, int n,

@@ -33,6 +33,7 @@ class _Problem(C.Structure):
         ("hh", C.c_void_p), ("inv_k", C.c_double * 4), ("orientation", C.c_double * 3),
         ("depth_near", C.c_double), ("depth_far", C.c_double), ("sp_alpha", C.c_float),
         ("seed", C.c_uint64), ("batch_id", C.c_uint32), ("quirks", C.c_int),
+        ("sampler", C.c_int),
     ]
 
 
@@ -54,6 +55,7 @@ def load(fp32: bool = False) -> C.CDLL:
     lib.pmo_prefilter.restype = C.c_int
     lib.pmo_prefilter.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_float, P]
     lib.pmo_box_moments.argtypes = [P, C.c_int, C.c_int, C.c_int, P, P]
+    lib.pmo_sample.argtypes = [P, C.c_int, C.c_int, P, P, P]
     lib.pmo_ncc.restype = C.c_double
     lib.pmo_ncc.argtypes = [P, P, P, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int]
     lib.pmo_ncc_batch.argtypes = [P, P, P, C.c_int, P, P, P, P, P, P]
@@ -135,7 +137,7 @@ class Oracle:
     def __init__(self, ref: np.ndarray, sources: list[np.ndarray], hh: np.ndarray, inv_k,
                  half_window: int, depth_near: float, depth_far: float, sp_alpha: float, seed: int,
                  orientation=(0.0, 0.0, 1.0), quirks: bool = True, batch_id: int = 0,
-                 fp32: bool = False):
+                 fp32: bool = False, sampler: int = 0):
         self.lib = load(fp32)
         self.ref = np.ascontiguousarray(ref, np.float32)
         self.sources = [np.ascontiguousarray(s, np.float32) for s in sources]
@@ -156,6 +158,7 @@ class Oracle:
         p.depth_near, p.depth_far = depth_near, depth_far
         p.sp_alpha = sp_alpha
         p.seed, p.batch_id, p.quirks = seed, batch_id, int(quirks)
+        p.sampler = int(sampler)
         self.p = p
         self.half_window = half_window
         self.sum_i, self.sum_ii = box_moments(self.ref, half_window, fp32)
@@ -167,6 +170,13 @@ class Oracle:
     def set_moments(self, sum_i, sum_ii):
         self.sum_i = np.ascontiguousarray(sum_i, np.float64)
         self.sum_ii = np.ascontiguousarray(sum_ii, np.float64)
+
+    def sample(self, view, xs, ys) -> np.ndarray:
+        xs = np.ascontiguousarray(xs, np.float32)
+        ys = np.ascontiguousarray(ys, np.float32)
+        out = np.empty(xs.shape, np.float64)
+        self.lib.pmo_sample(self._pp, view, xs.size, xs.ctypes.data, ys.ctypes.data, out.ctypes.data)
+        return out
 
     def ncc(self, x, y, view, depth, axis) -> float:
         return self.lib.pmo_ncc(self._pp, self.sum_i.ctypes.data, self.sum_ii.ctypes.data, x, y, view, depth, axis)
@@ -237,4 +247,4 @@ def from_images(images, ref_id: int, params, source_texels=None, ref_texels=None
     src_t = source_texels if source_texels is not None else [texels(s) for s in srcs]
     return Oracle(ref_t, src_t, np.array(hh), ik, params.half_window, params.depth_near, params.depth_far,
                   params.sp_alpha, params.seed, (params.orientation_x, 0.0, params.orientation_z),
-                  bool(params.quirks), 0, fp32)
+                  bool(params.quirks), 0, fp32, getattr(params, "sampler", 0))

@@ -111,21 +111,25 @@ __device__ __forceinline__ float warp_sum(float v)
 }
 
 // HMM messages (patchMatch.cu:669-715). e = exp(-c^2 / (2 a2)); a cost of exactly 2 is
-// replaced by 2 U(0,1] by the caller.
-__device__ __forceinline__ float emission(float c, float a2) { return expf(-0.5f * c * c / a2); }
+// replaced by 2 U(0,1] by the caller. The reference stores emissions and messages in float
+// and builds with --use_fast_math, so values below the smallest normal float become zero;
+// ftz() keeps that behaviour whatever the compiler's denormal mode.
+__device__ __forceinline__ float ftz(float x) { return fabsf(x) < 1.17549435e-38f ? 0.0f : x; }
+
+__device__ __forceinline__ float emission(float c, float a2) { return ftz(expf(-0.5f * c * c / a2)); }
 
 __device__ __forceinline__ float msg_backward(float m, float e, float u)
 {
     const float zn0 = m * e * FIX_STATE_PROB + (1.0f - m) * u * CHANGE_STATE_PROB;
     const float zn1 = m * e * CHANGE_STATE_PROB + (1.0f - m) * u * FIX_STATE_PROB;
-    return zn0 / (zn0 + zn1);
+    return ftz(zn0 / (zn0 + zn1));
 }
 
 __device__ __forceinline__ float msg_forward(float m, float e, float u)
 {
     const float zn0 = (m * FIX_STATE_PROB + (1.0f - m) * CHANGE_STATE_PROB) * e;
     const float zn1 = (m * CHANGE_STATE_PROB + (1.0f - m) * FIX_STATE_PROB) * u;
-    return zn0 / (zn0 + zn1);
+    return ftz(zn0 / (zn0 + zn1));
 }
 
 // ---- window slots ---------------------------------------------------------------------------

@@ -140,7 +140,7 @@ sweep_kernel(const __grid_constant__ SweepArgs A)
             if (c == 2.0f) c = 2.0f * draw_uniform(seed, pix, sweep, RNG_FWD_PRE, lane, batch);
             const float a = msg_forward(alpha, emission(c, a2), u_emit);
             const float z0 = a * b, z1 = (1.0f - a) * (1.0f - b);
-            q = z0 / (z0 + z1);
+            q = ftz(z0 / (z0 + z1));
         }
         float cdf = q;
 #pragma unroll

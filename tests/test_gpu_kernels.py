@@ -71,6 +71,49 @@ def test_source_sampling_exact_bilinear(small_scene, prefilter, precision):
     eng.close()
 
 
+@pytest.mark.parametrize("texel_format,tol", [(4, 2e-7), (1, 2e-5)])
+def test_hardware_sampler_matches_fixed_point_model(small_scene, texel_format, tol, parity_log):
+    """Texture-unit bilinear filtering equals the oracle's fixed-point model: fractions and
+    their product rounded half-up to 1/256 (FP32 texels exactly; u8 texels to the filter's
+    output precision, about 2^-17)."""
+    over = dict(sampler=1, texel_format=texel_format, prefilter=1 if texel_format == 4 else 0)
+    eng = make_engine(small_scene, **over)
+    orc = oracle_for(eng, small_scene, small_scene.workload.params(**over))
+    rng = np.random.default_rng(5)
+    h, w = eng.source_texels(2).shape
+    xs = rng.uniform(-2, w + 1, 20000).astype(np.float32)
+    ys = rng.uniform(-2, h + 1, 20000).astype(np.float32)
+    got = eng.sample_source(2, xs, ys)
+    err = np.abs(got - orc.sample(2, xs, ys))
+    parity_log(f"hw_sampler_texels{texel_format}", err_max=float(err.max()))
+    assert err.max() <= tol
+    eng.close()
+
+
+@pytest.mark.parametrize("texel_format", [4, 1])
+def test_ncc_parity_hardware_sampler(small_scene, texel_format, parity_log):
+    """NCC through texture-unit filtering against the oracle's fixed-point model. The GPU forms
+    source coordinates in FP32, so near a 1/256 weight boundary it can round a fraction the
+    other way than the FP64 oracle; the bound reflects those single-step weight flips."""
+    over = dict(sampler=1, texel_format=texel_format, prefilter=1 if texel_format == 4 else 0)
+    eng = make_engine(small_scene, **over)
+    orc = oracle_for(eng, small_scene, small_scene.workload.params(**over))
+    rng = np.random.default_rng(6)
+    n = 4096
+    w = small_scene.workload
+    xs = rng.integers(0, w.width, n)
+    ys = rng.integers(0, w.height, n)
+    vs = rng.integers(0, w.n_src, n)
+    gt = small_scene.gt_depth[ys, xs]
+    ds = np.where(rng.random(n) < 0.5, gt, rng.uniform(w.depth_near, w.depth_far, n)).astype(np.float32)
+    ax = rng.integers(0, 2, n)
+    err = ncc_err(eng.eval_costs(xs, ys, vs, ds, ax), orc.ncc_batch(xs, ys, vs, ds, ax))
+    parity_log(f"ncc_hw_texels{texel_format}", err_max=float(err.max()), err_q999=float(np.quantile(err, 0.999)),
+               err_median=float(np.median(err)))
+    assert np.quantile(err, 0.999) <= 5 * NCC_TOL and err.max() <= 20 * NCC_TOL
+    eng.close()
+
+
 def test_u8_texels_are_unorm(small_scene):
     eng = make_engine(small_scene, prefilter=0)
     src = [im for i, im in enumerate(small_scene.images) if i != small_scene.ref_id][0]
