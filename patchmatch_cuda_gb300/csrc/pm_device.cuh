@@ -153,12 +153,12 @@ struct Window {
 template <int W>
 struct PixelWindow {
     static constexpr int NS = Window<W>::NS;
-    float b[NS];         // R - mu for the slot's paired reference value (in-bounds slots)
+    float *b;            // this warp's shared table: b[32 * i + lane] = R - mu of slot i
     uint64_t inb;        // slot in bounds
     float ox, oy;        // window origin in reference pixel-centre coordinates
     float n, inv_n;      // in-bounds count
     float c1;            // reference variance term, clamped
-    float bsum;          // sum over in-bounds slots of (R - mu)
+    float bsum;          // sum over in-bounds slots of (R_paired - mu); 0 when aligned
     float scale;         // plane scale at this pixel
 };
 
@@ -166,7 +166,7 @@ struct PixelWindow {
 // column axis for the reference's misalignment (0: x, vertical sweeps; 1: y).
 template <int W>
 __device__ __forceinline__ void load_window(const RefDesc &D, int x, int y, int axis, int lane,
-                                            const float2 *slots, PixelWindow<W> &pw)
+                                            const float2 *slots, float *btab, PixelWindow<W> &pw)
 {
     constexpr int HW = Window<W>::HW, NS = Window<W>::NS, NSAMP = Window<W>::NSAMP;
     const int Wd = D.width, Hd = D.height;
@@ -185,6 +185,7 @@ __device__ __forceinline__ void load_window(const RefDesc &D, int x, int y, int 
     pw.c1 = __ldg(D.c1 + pix);
     uint64_t inb = 0;
     float bs = 0.0f;
+    const bool shifted = (lead_x | lead_y) != 0;
 #pragma unroll
     for (int i = 0; i < NS; ++i) {
         const int k = lane + 32 * i;
@@ -193,16 +194,24 @@ __device__ __forceinline__ void load_window(const RefDesc &D, int x, int y, int 
         const bool in = (k < NSAMP) && xx >= 0 && xx < Wd && yy >= 0 && yy < Hd;
         float r = 0.0f;
         if (in) {
-            const int rx = xx - lead_x, ry = yy - lead_y;
-            if (rx >= 0 && ry >= 0) r = __ldg(D.ref + (size_t)ry * Wd + rx);
+            r = __ldg(D.ref + (size_t)yy * Wd + xx);
+            if (shifted) {
+                // the reference pairs this source sample with a reference value shifted
+                // back over the leading out-of-bounds columns (zero outside the image)
+                const int rx = xx - lead_x, ry = yy - lead_y;
+                const float rm = (rx >= 0 && ry >= 0) ? __ldg(D.ref + (size_t)ry * Wd + rx) : 0.0f;
+                bs += rm - r;
+                r = rm;
+            }
             inb |= (uint64_t)1 << i;
             r -= mu;
-            bs += r;
         }
-        pw.b[i] = r;
+        btab[32 * i + lane] = r;
     }
+    pw.b = btab;
     pw.inb = inb;
-    pw.bsum = warp_sum(bs);
+    // sum(R_paired - mu) = sum(R_paired) - sum(R): exactly zero for aligned windows
+    pw.bsum = shifted ? warp_sum(bs) : 0.0f;
     pw.ox = (float)x0 + 0.5f;
     pw.oy = (float)y0 + 0.5f;
     pw.scale = D.nx * (D.ik00 * ((float)x + 0.5f) + D.ik02) + D.nz;
@@ -315,8 +324,9 @@ __device__ __forceinline__ void eval_pair(const RefDesc &D, const PixelWindow<W>
     for (int i = 0; i < NS; ++i) {
         if (pw.inb & ((uint64_t)1 << i)) {
             const float ea = sa[i] - ma, eb = sb[i] - mb;
-            qa = fmaf(ea, ea, qa); xa = fmaf(ea, pw.b[i], xa);
-            qb = fmaf(eb, eb, qb); xb = fmaf(eb, pw.b[i], xb);
+            const float bi = pw.b[32 * i + lane];
+            qa = fmaf(ea, ea, qa); xa = fmaf(ea, bi, xa);
+            qb = fmaf(eb, eb, qb); xb = fmaf(eb, bi, xb);
         }
     }
     qa = warp_sum(qa); xa = warp_sum(xa);
@@ -363,7 +373,7 @@ __device__ __forceinline__ float eval_one(const RefDesc &D, const PixelWindow<W>
     for (int i = 0; i < NS; ++i) {
         if (pw.inb & ((uint64_t)1 << i)) {
             const float ea = sa[i] - ma;
-            qa = fmaf(ea, ea, qa); xa = fmaf(ea, pw.b[i], xa);
+            qa = fmaf(ea, ea, qa); xa = fmaf(ea, pw.b[32 * i + lane], xa);
         }
     }
     qa = warp_sum(qa); xa = warp_sum(xa);

@@ -48,7 +48,7 @@ __device__ __forceinline__ int nth_bit(unsigned m, int t)
 }
 
 template <int W>
-__global__ void __launch_bounds__(32 * MAX_WARPS_PER_LINE)
+__global__ void __launch_bounds__(32 * MAX_WARPS_PER_LINE, 5)
 sweep_kernel(const __grid_constant__ SweepArgs A)
 {
     constexpr int NS = Window<W>::NS;
@@ -78,6 +78,8 @@ sweep_kernel(const __grid_constant__ SweepArgs A)
     __shared__ float s_new[MAX_VIEWS];       // refreshed costs
 
     __shared__ float2 slots[32 * NS];
+    __shared__ float btabs[MAX_WARPS_PER_LINE][32 * NS];
+    float *btab = btabs[warp];
     fill_slot_table<W>(slots);
     __syncthreads();
 
@@ -131,7 +133,7 @@ sweep_kernel(const __grid_constant__ SweepArgs A)
         const float b = vl ? bline[(size_t)k * V + lane] : 0.0f;
         const float d_cur = D.depth[pix];
         PixelWindow<W> pw;
-        load_window<W>(D, x, y, axis, lane, slots, pw);
+        load_window<W>(D, x, y, axis, lane, slots, btab, pw);
 
         // forward message with the old costs, posterior, CDF (:905-923)
         float q = 0.0f;
@@ -263,13 +265,15 @@ __global__ void __launch_bounds__(COST_BLOCK) costs_kernel(const RefDesc *refs, 
     const int V = D.n_src;
     const int npix = D.width * D.height;
     __shared__ float2 slots[32 * NS];
+    __shared__ float btabs[COST_BLOCK / 32][32 * NS];
+    float *btab = btabs[threadIdx.x >> 5];
     fill_slot_table<W>(slots);
     __syncthreads();
     const int warps = (int)((gridDim.x * blockDim.x) >> 5);
     for (int p = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); p < npix; p += warps) {
         const int x = p % D.width, y = p / D.width;
         PixelWindow<W> pw;
-        load_window<W>(D, x, y, axis, lane, slots, pw);
+        load_window<W>(D, x, y, axis, lane, slots, btab, pw);
         const float d = D.depth[p];
         float mine = 0.0f;
         for (int v = 0; v + 1 < V; v += 2) {
@@ -300,13 +304,15 @@ __global__ void __launch_bounds__(COST_BLOCK) eval_kernel(const RefDesc *refs, i
     const RefDesc &D = refs[r];
     const int lane = threadIdx.x & 31;
     __shared__ float2 slots[32 * NS];
+    __shared__ float btabs[COST_BLOCK / 32][32 * NS];
+    float *btab = btabs[threadIdx.x >> 5];
     fill_slot_table<W>(slots);
     __syncthreads();
     const int warps = (int)((gridDim.x * blockDim.x) >> 5);
     for (int i = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); i < n; i += warps) {
         const int4 t = q[i];  // x, y, view, axis
         PixelWindow<W> pw;
-        load_window<W>(D, t.x, t.y, t.w, lane, slots, pw);
+        load_window<W>(D, t.x, t.y, t.w, lane, slots, btab, pw);
         const float v = eval_one<W>(D, pw, slots, lane, t.z, depths[i]);
         if (lane == 0) out[i] = v;
     }
