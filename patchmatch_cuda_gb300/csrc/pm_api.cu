@@ -206,6 +206,8 @@ cudaError_t dalloc(T **p, size_t bytes, cudaStream_t s)
 
 int window_side(const pm_handle *h) { return 2 * h->p.half_window + 1; }
 
+bool hw_of(const pm_handle *h) { return h->p.sampler == PM_SAMPLER_HARDWARE; }
+
 cudaError_t enqueue_costs(pm_handle *h, int axis)
 {
     LaunchReq req{};
@@ -216,7 +218,7 @@ cudaError_t enqueue_costs(pm_handle *h, int axis)
     req.axis = axis;
     const int npix = h->W * h->H;
     req.grid = (npix + COST_BLOCK / 32 - 1) / (COST_BLOCK / 32);
-    return launch_window(window_side(h), req);
+    return launch_window(window_side(h), h->p.sampler == PM_SAMPLER_HARDWARE, req);
 }
 
 void fill_sweep_args(SweepArgs &a, const RefDesc *refs, const int *lines, int nrefs, int dir,
@@ -233,7 +235,7 @@ void fill_sweep_args(SweepArgs &a, const RefDesc *refs, const int *lines, int nr
     a.total_lines = a.line_start[nrefs];
 }
 
-cudaError_t enqueue_sweep(int win, int wpl, const SweepArgs &a, cudaStream_t s)
+cudaError_t enqueue_sweep(int win, bool hw, int wpl, const SweepArgs &a, cudaStream_t s)
 {
     if (a.total_lines == 0) return cudaSuccess;
     LaunchReq req{};
@@ -242,7 +244,7 @@ cudaError_t enqueue_sweep(int win, int wpl, const SweepArgs &a, cudaStream_t s)
     req.sweep = &a;
     req.grid = a.total_lines;
     req.block = 32 * wpl;
-    return launch_window(win, req);
+    return launch_window(win, hw, req);
 }
 
 inline int orient(int dir) { return (dir == PM_DIR_LEFT_TO_RIGHT || dir == PM_DIR_RIGHT_TO_LEFT) ? 1 : 0; }
@@ -297,7 +299,7 @@ cudaError_t enqueue_schedule(pm_handle *h)
             const int lines = lines_of(h, d);
             fill_sweep_args(a, h->d_desc, &lines, 1, d, (uint32_t)(4 * it + d), it == 0 ? 1 : 0,
                             (it == iters - 1 && d == PM_DIR_BOTTOM_TO_TOP) ? 1 : 0);
-            e = enqueue_sweep(window_side(h), h->wpl[orient(d)], a, h->stream);
+            e = enqueue_sweep(window_side(h), hw_of(h), h->wpl[orient(d)], a, h->stream);
             if (e != cudaSuccess) return e;
         }
     return cudaSuccess;
@@ -335,7 +337,7 @@ cudaError_t tune_warps_per_line(pm_handle *h)
                 float ms = 0.0f;
                 for (int rep = 0; rep < 2; ++rep) {  // first launch warms caches
                     e = cudaEventRecord(h->ev[2], h->stream);
-                    if (e == cudaSuccess) e = enqueue_sweep(h->win, wpl, a, h->stream);
+                    if (e == cudaSuccess) e = enqueue_sweep(h->win, hw_of(h), wpl, a, h->stream);
                     if (e == cudaSuccess) e = cudaEventRecord(h->ev[3], h->stream);
                     if (e == cudaSuccess) e = cudaEventSynchronize(h->ev[3]);
                     if (e != cudaSuccess) return e;
@@ -352,7 +354,7 @@ cudaError_t tune_warps_per_line(pm_handle *h)
 }
 
 // Warps per line for a batched launch: the most that still keeps every line resident.
-int batch_wpl(int win, int total_lines, int device)
+int batch_wpl(int win, bool hw, int total_lines, int device)
 {
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
@@ -362,7 +364,7 @@ int batch_wpl(int win, int total_lines, int device)
         r.kind = LaunchKind::SweepOccupancy;
         r.block = 32 * wpl;
         r.occupancy = &occ;
-        if (launch_window(win, r) == cudaSuccess && total_lines <= occ * sms) return wpl;
+        if (launch_window(win, hw, r) == cudaSuccess && total_lines <= occ * sms) return wpl;
     }
     return 1;
 }
@@ -723,13 +725,16 @@ pm_status pm_run_batch(pm_handle *const *hs, int n)
     if (st != PM_OK) return st;
     for (int i = 0; i < n; ++i) PM_CUDA(hs[i], cudaStreamSynchronize(hs[i]->stream));
     cudaStream_t s = h0->stream;
-    // group by window side; each group sweeps in one launch per direction
+    // group by window side and sampler; each group sweeps in one launch per direction
     std::vector<int> done(n, 0);
     for (int g0 = 0; g0 < n; ++g0) {
         if (done[g0]) continue;
         std::vector<pm_handle *> grp;
         for (int i = g0; i < n; ++i)
-            if (!done[i] && hs[i]->win == hs[g0]->win) { grp.push_back(hs[i]); done[i] = 1; }
+            if (!done[i] && hs[i]->win == hs[g0]->win && hw_of(hs[i]) == hw_of(hs[g0])) {
+                grp.push_back(hs[i]);
+                done[i] = 1;
+            }
         for (size_t start = 0; start < grp.size(); start += MAX_BATCH_REFS) {
             const int m = (int)std::min<size_t>(MAX_BATCH_REFS, grp.size() - start);
             RefDesc *d_descs = nullptr;
@@ -748,7 +753,7 @@ pm_status pm_run_batch(pm_handle *const *hs, int n)
                 req.ref_index = i;
                 req.axis = 1;
                 req.grid = (h->W * h->H + COST_BLOCK / 32 - 1) / (COST_BLOCK / 32);
-                PM_CUDA(h0, launch_window(h->win, req));
+                PM_CUDA(h0, launch_window(h->win, hw_of(h), req));
                 max_iters = std::max(max_iters, h->p.num_iterations);
             }
             std::vector<SweepArgs> args((size_t)max_iters * 4);
@@ -762,7 +767,7 @@ pm_status pm_run_batch(pm_handle *const *hs, int n)
                     SweepArgs &a = args[(size_t)it * 4 + d];
                     fill_sweep_args(a, d_descs, lines.data(), m, d, (uint32_t)(4 * it + d),
                                     it == 0 ? 1 : 0, d == PM_DIR_BOTTOM_TO_TOP ? 1 : 0);
-                    PM_CUDA(h0, enqueue_sweep(grp[start]->win, batch_wpl(grp[start]->win, a.total_lines, h0->device), a, s));
+                    PM_CUDA(h0, enqueue_sweep(grp[start]->win, hw_of(grp[start]), batch_wpl(grp[start]->win, hw_of(grp[start]), a.total_lines, h0->device), a, s));
                 }
             PM_CUDA(h0, cudaFreeAsync(d_descs, s));
         }
@@ -883,7 +888,7 @@ pm_status pm_run_sweep(pm_handle *h, int direction, uint32_t sweep_id, int num_s
         PM_CUDA(h, cudaMemcpyAsync(h->d_cost, c.data(), c.size() * 4, cudaMemcpyHostToDevice, h->stream));
     }
     PM_CUDA(h, cudaEventRecord(h->ev[2], h->stream));
-    PM_CUDA(h, enqueue_sweep(h->win, h->wpl[orient(direction)], a, h->stream));
+    PM_CUDA(h, enqueue_sweep(h->win, hw_of(h), h->wpl[orient(direction)], a, h->stream));
     PM_CUDA(h, cudaEventRecord(h->ev[3], h->stream));
     PM_CUDA(h, cudaStreamSynchronize(h->stream));
     float ms = 0.0f;
@@ -994,7 +999,7 @@ pm_status pm_eval_costs(pm_handle *h, int n, const int *xs, const int *ys, const
     req.depths = d_d;
     req.out = d_o;
     req.grid = std::min((n + COST_BLOCK / 32 - 1) / (COST_BLOCK / 32), 65535);
-    PM_CUDA(h, launch_window(h->win, req));
+    PM_CUDA(h, launch_window(h->win, hw_of(h), req));
     PM_CUDA(h, cudaMemcpyAsync(out, d_o, sizeof(float) * n, cudaMemcpyDeviceToHost, s));
     PM_CUDA(h, cudaFreeAsync(d_q, s));
     PM_CUDA(h, cudaFreeAsync(d_d, s));

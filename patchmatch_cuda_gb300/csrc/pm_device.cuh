@@ -155,6 +155,7 @@ struct PixelWindow {
     static constexpr int NS = Window<W>::NS;
     float *b;            // this warp's shared table: b[32 * i + lane] = R - mu of slot i
     uint64_t inb;        // slot in bounds
+    bool full;           // the whole window lies inside the reference image
     float ox, oy;        // window origin in reference pixel-centre coordinates
     float n, inv_n;      // in-bounds count
     float c1;            // reference variance term, clamped
@@ -179,6 +180,7 @@ __device__ __forceinline__ void load_window(const RefDesc &D, int x, int y, int 
     const int cx0 = max(x0, 0), cx1 = min(x + HW, Wd - 1);
     const int cy0 = max(y0, 0), cy1 = min(y + HW, Hd - 1);
     pw.n = (float)((cx1 - cx0 + 1) * (cy1 - cy0 + 1));
+    pw.full = x0 >= 0 && y0 >= 0 && x + HW < Wd && y + HW < Hd;
     pw.inv_n = 1.0f / pw.n;
     const size_t pix = (size_t)y * Wd + x;
     const float mu = __ldg(D.sum_i + pix) / pw.n;
@@ -224,9 +226,9 @@ __device__ __forceinline__ float ncc_finalize(float sj, float c2, float x, float
 {
     if (sj == 0.0f) return 2.0f;
     c2 = c2 < 0.00001f ? 0.0f : c2;
-    const float c = sqrtf(c1 * c2);
-    if (c == 0.0f) return 1.0f;
-    return 1.0f - fmaf(mu_j, bsum, x) / c;
+    const float cc = c1 * c2;
+    if (cc == 0.0f) return 1.0f;
+    return 1.0f - fmaf(mu_j, bsum, x) * rsqrtf(cc);
 }
 
 // Plane-induced homography of (view, depth) applied at the window origin:
@@ -236,6 +238,7 @@ struct WarpSetup {
     float c0x, c0y, c0z, c1x, c1y, c1z, bx, by, bz;
 };
 
+template <bool HW>
 __device__ __forceinline__ WarpSetup warp_setup(const RefDesc &D, int view, float depth,
                                                 float scale, float ox, float oy)
 {
@@ -245,10 +248,18 @@ __device__ __forceinline__ WarpSetup warp_setup(const RefDesc &D, int view, floa
     // 20 floats per view: H1 (row-major, floats 0-8), H2 (floats 9-17), 2 pad.
     const float h1[9] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x};
     const float h2[9] = {c.y, c.z, c.w, d.x, d.y, d.z, d.w, e.x, e.y};
-    const float s = 1.0f / (depth * scale);
+    const float s = __fdividef(1.0f, depth * scale);
     float t[9];
 #pragma unroll
     for (int i = 0; i < 9; ++i) t[i] = fmaf(-s, h2[i], h1[i]);
+    if (HW) {
+        // texture coordinates are (u/z + 1/2, v/z + 1/2): add z/2 to the first two rows
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            t[i] = fmaf(0.5f, t[6 + i], t[i]);
+            t[3 + i] = fmaf(0.5f, t[6 + i], t[3 + i]);
+        }
+    }
     WarpSetup w;
     w.c0x = t[0]; w.c0y = t[3]; w.c0z = t[6];
     w.c1x = t[1]; w.c1y = t[4]; w.c1z = t[7];
@@ -266,118 +277,110 @@ __device__ __forceinline__ float warp_sample(const WarpSetup &A, cudaTextureObje
     const float py = fmaf(A.c0y, dx, fmaf(A.c1y, dy, A.by));
     float pz = fmaf(A.c0z, dx, fmaf(A.c1z, dy, A.bz));
     if (HW) {
-        // keep the coordinate finite on the source camera's principal plane (border -> 0)
+        // keep the coordinate finite on the source camera's principal plane (border -> 0);
+        // px, py already carry the texture's half-texel offset
         pz = fabsf(pz) < 1e-20f ? 1e-20f : pz;
         const float r = __fdividef(1.0f, pz);
-        return sample_source_hw(tex, px * r, py * r);
+        return tex2D<float>(tex, px * r, py * r);
     }
     const float r = __fdividef(1.0f, pz);
     return sample_source(tex, px * r, py * r, sw, sh);
 }
 
-// Two windowed NCC evaluations (views va/vb at depths da/db) for one pixel; every lane
-// returns both results. The samples stay in registers for the centred second pass.
+// Whether lane `lane`'s slot i is a window sample: the window may not fill the last slot.
 template <int W>
+__device__ __forceinline__ bool slot_exists(int i, int lane)
+{
+    return i < Window<W>::NS - 1 || lane + 32 * i < Window<W>::NSAMP;
+}
+
+// E windowed NCC evaluations (views v[e] at depths d[e], E = 1 or 2) for one pixel; every
+// lane returns the results. Source samples stay in registers for the centred second pass.
+// FULL: the window lies inside the image, so only the last slot needs a test.
+template <int W, int E, bool HW, bool FULL>
+__device__ __forceinline__ void eval_core(const RefDesc &D, const PixelWindow<W> &pw,
+                                          const float2 *slots, int lane, const int (&v)[E],
+                                          const float (&d)[E], float (&out)[E])
+{
+    constexpr int NS = Window<W>::NS;
+    WarpSetup A[E];
+    cudaTextureObject_t tex[E];
+    float sw[E], sh[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        A[e] = warp_setup<HW>(D, v[e], d[e], pw.scale, pw.ox, pw.oy);
+        tex[e] = D.tex[v[e]];
+        sw[e] = D.src_w[v[e]];
+        sh[e] = D.src_h[v[e]];
+    }
+    float smp[E][NS];
+    float j[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) j[e] = 0.f;
+#pragma unroll
+    for (int i = 0; i < NS; ++i) {
+        const bool take = FULL ? slot_exists<W>(i, lane) : ((pw.inb >> i) & 1) != 0;
+        const float2 o = slots[32 * i + lane];
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            smp[e][i] = 0.f;
+            if (take) {
+                smp[e][i] = warp_sample<HW>(A[e], tex[e], sw[e], sh[e], o.x, o.y);
+                j[e] += smp[e][i];
+            }
+        }
+    }
+    float m[E], q[E], x[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        j[e] = warp_sum(j[e]);
+        m[e] = j[e] * pw.inv_n;
+        q[e] = 0.f;
+        x[e] = 0.f;
+    }
+#pragma unroll
+    for (int i = 0; i < NS; ++i) {
+        const bool take = FULL ? slot_exists<W>(i, lane) : ((pw.inb >> i) & 1) != 0;
+        if (take) {
+            const float bi = pw.b[32 * i + lane];
+#pragma unroll
+            for (int e = 0; e < E; ++e) {
+                const float de = smp[e][i] - m[e];
+                q[e] = fmaf(de, de, q[e]);
+                x[e] = fmaf(de, bi, x[e]);
+            }
+        }
+    }
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        q[e] = warp_sum(q[e]);
+        x[e] = warp_sum(x[e]);
+        out[e] = ncc_finalize(j[e], q[e], x[e], pw.c1, m[e], pw.bsum);
+    }
+}
+
+template <int W, bool HW>
+__device__ __forceinline__ float eval_one(const RefDesc &D, const PixelWindow<W> &pw,
+                                          const float2 *slots, int lane, int v, float d)
+{
+    const int vv[1] = {v};
+    const float dd[1] = {d};
+    float out[1];
+    eval_core<W, 1, HW, false>(D, pw, slots, lane, vv, dd, out);
+    return out[0];
+}
+
+template <int W, bool HW>
 __device__ __forceinline__ void eval_pair(const RefDesc &D, const PixelWindow<W> &pw,
                                           const float2 *slots, int lane, int va, float da,
                                           int vb, float db, float &out_a, float &out_b)
 {
-    constexpr int NS = Window<W>::NS;
-    const WarpSetup A = warp_setup(D, va, da, pw.scale, pw.ox, pw.oy);
-    const WarpSetup B = warp_setup(D, vb, db, pw.scale, pw.ox, pw.oy);
-    const cudaTextureObject_t ta = D.tex[va], tb = D.tex[vb];
-    const float swa = D.src_w[va], sha = D.src_h[va], swb = D.src_w[vb], shb = D.src_h[vb];
-    float sa[NS], sb[NS];
-    float ja = 0.f, jb = 0.f;
-    if (D.hw_filter) {
-#pragma unroll
-        for (int i = 0; i < NS; ++i) {
-            sa[i] = 0.f;
-            sb[i] = 0.f;
-            if (pw.inb & ((uint64_t)1 << i)) {
-                const float2 o = slots[32 * i + lane];
-                sa[i] = warp_sample<true>(A, ta, swa, sha, o.x, o.y);
-                sb[i] = warp_sample<true>(B, tb, swb, shb, o.x, o.y);
-                ja += sa[i];
-                jb += sb[i];
-            }
-        }
-    } else {
-#pragma unroll
-        for (int i = 0; i < NS; ++i) {
-            sa[i] = 0.f;
-            sb[i] = 0.f;
-            if (pw.inb & ((uint64_t)1 << i)) {
-                const float2 o = slots[32 * i + lane];
-                sa[i] = warp_sample<false>(A, ta, swa, sha, o.x, o.y);
-                sb[i] = warp_sample<false>(B, tb, swb, shb, o.x, o.y);
-                ja += sa[i];
-                jb += sb[i];
-            }
-        }
-    }
-    ja = warp_sum(ja);
-    jb = warp_sum(jb);
-    const float ma = ja * pw.inv_n, mb = jb * pw.inv_n;
-    float qa = 0.f, xa = 0.f, qb = 0.f, xb = 0.f;
-#pragma unroll
-    for (int i = 0; i < NS; ++i) {
-        if (pw.inb & ((uint64_t)1 << i)) {
-            const float ea = sa[i] - ma, eb = sb[i] - mb;
-            const float bi = pw.b[32 * i + lane];
-            qa = fmaf(ea, ea, qa); xa = fmaf(ea, bi, xa);
-            qb = fmaf(eb, eb, qb); xb = fmaf(eb, bi, xb);
-        }
-    }
-    qa = warp_sum(qa); xa = warp_sum(xa);
-    qb = warp_sum(qb); xb = warp_sum(xb);
-    out_a = ncc_finalize(ja, qa, xa, pw.c1, ma, pw.bsum);
-    out_b = ncc_finalize(jb, qb, xb, pw.c1, mb, pw.bsum);
-}
-
-template <int W>
-__device__ __forceinline__ float eval_one(const RefDesc &D, const PixelWindow<W> &pw,
-                                          const float2 *slots, int lane, int v, float d)
-{
-    constexpr int NS = Window<W>::NS;
-    const WarpSetup A = warp_setup(D, v, d, pw.scale, pw.ox, pw.oy);
-    const cudaTextureObject_t ta = D.tex[v];
-    const float sw = D.src_w[v], sh = D.src_h[v];
-    float sa[NS];
-    float ja = 0.f;
-    if (D.hw_filter) {
-#pragma unroll
-        for (int i = 0; i < NS; ++i) {
-            sa[i] = 0.f;
-            if (pw.inb & ((uint64_t)1 << i)) {
-                const float2 o = slots[32 * i + lane];
-                sa[i] = warp_sample<true>(A, ta, sw, sh, o.x, o.y);
-                ja += sa[i];
-            }
-        }
-    } else {
-#pragma unroll
-        for (int i = 0; i < NS; ++i) {
-            sa[i] = 0.f;
-            if (pw.inb & ((uint64_t)1 << i)) {
-                const float2 o = slots[32 * i + lane];
-                sa[i] = warp_sample<false>(A, ta, sw, sh, o.x, o.y);
-                ja += sa[i];
-            }
-        }
-    }
-    ja = warp_sum(ja);
-    const float ma = ja * pw.inv_n;
-    float qa = 0.f, xa = 0.f;
-#pragma unroll
-    for (int i = 0; i < NS; ++i) {
-        if (pw.inb & ((uint64_t)1 << i)) {
-            const float ea = sa[i] - ma;
-            qa = fmaf(ea, ea, qa); xa = fmaf(ea, pw.b[32 * i + lane], xa);
-        }
-    }
-    qa = warp_sum(qa); xa = warp_sum(xa);
-    return ncc_finalize(ja, qa, xa, pw.c1, ma, pw.bsum);
+    const int vv[2] = {va, vb};
+    const float dd[2] = {da, db};
+    float out[2];
+    eval_core<W, 2, HW, false>(D, pw, slots, lane, vv, dd, out);
+    out_a = out[0];
+    out_b = out[1];
 }
 
 // Window offsets (dx, dy) of every lane's slots: table[32 * i + lane] for slot i, filled

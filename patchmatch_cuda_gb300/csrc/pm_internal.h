@@ -28,15 +28,26 @@ struct LaunchReq {
     float *out;
 };
 
-// Window-size dispatch, split over translation units so they compile in parallel.
-// Each returns cudaErrorInvalidValue when W is not in its group.
-cudaError_t launch_group_a(int W, const LaunchReq &req);  // 3 .. 11
-cudaError_t launch_group_b(int W, const LaunchReq &req);  // 13 .. 17
-cudaError_t launch_group_c(int W, const LaunchReq &req);  // 19 .. 25
-cudaError_t launch_group_d(int W, const LaunchReq &req);  // 27 .. 45
+// Window-size and sampler dispatch, split over translation units so they compile in
+// parallel. Each returns cudaErrorInvalidValue when W is not in its group. The _hw groups
+// sample through texture-unit bilinear filtering, the others through exact gathers.
+cudaError_t launch_group_a(int W, const LaunchReq &req);     // 3 .. 11
+cudaError_t launch_group_b(int W, const LaunchReq &req);     // 13 .. 17
+cudaError_t launch_group_c(int W, const LaunchReq &req);     // 19 .. 25
+cudaError_t launch_group_d(int W, const LaunchReq &req);     // 27 .. 45
+cudaError_t launch_group_a_hw(int W, const LaunchReq &req);
+cudaError_t launch_group_b_hw(int W, const LaunchReq &req);
+cudaError_t launch_group_c_hw(int W, const LaunchReq &req);
+cudaError_t launch_group_d_hw(int W, const LaunchReq &req);
 
-inline cudaError_t launch_window(int W, const LaunchReq &req)
+inline cudaError_t launch_window(int W, bool hw, const LaunchReq &req)
 {
+    if (hw) {
+        if (W <= 11) return launch_group_a_hw(W, req);
+        if (W <= 17) return launch_group_b_hw(W, req);
+        if (W <= 25) return launch_group_c_hw(W, req);
+        return launch_group_d_hw(W, req);
+    }
     if (W <= 11) return launch_group_a(W, req);
     if (W <= 17) return launch_group_b(W, req);
     if (W <= 25) return launch_group_c(W, req);

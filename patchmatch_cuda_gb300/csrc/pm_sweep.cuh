@@ -47,8 +47,8 @@ __device__ __forceinline__ int nth_bit(unsigned m, int t)
     return __ffs(m) - 1;
 }
 
-template <int W>
-__global__ void __launch_bounds__(32 * MAX_WARPS_PER_LINE, 5)
+template <int W, bool HW>
+__global__ void __launch_bounds__(32 * MAX_WARPS_PER_LINE, 4)
 sweep_kernel(const __grid_constant__ SweepArgs A)
 {
     constexpr int NS = Window<W>::NS;
@@ -189,7 +189,7 @@ sweep_kernel(const __grid_constant__ SweepArgs A)
                     d = best;
                     dst = &s_new[v];
                 }
-                const float res = eval_one<W>(D, pw, slots, lane, v, d);
+                const float res = eval_one<W, HW>(D, pw, slots, lane, v, d);
                 if (lane == 0) *dst = res;
             }
             if (phase == 1 && ntasks == 0) break;
@@ -256,7 +256,7 @@ sweep_kernel(const __grid_constant__ SweepArgs A)
 }
 
 // All views' costs at the current depth for every pixel of one reference.
-template <int W>
+template <int W, bool HW>
 __global__ void __launch_bounds__(COST_BLOCK) costs_kernel(const RefDesc *refs, int r, int axis)
 {
     constexpr int NS = Window<W>::NS;
@@ -278,12 +278,12 @@ __global__ void __launch_bounds__(COST_BLOCK) costs_kernel(const RefDesc *refs, 
         float mine = 0.0f;
         for (int v = 0; v + 1 < V; v += 2) {
             float na, nb;
-            eval_pair<W>(D, pw, slots, lane, v, d, v + 1, d, na, nb);
+            eval_pair<W, HW>(D, pw, slots, lane, v, d, v + 1, d, na, nb);
             if (lane == v) mine = na;
             if (lane == v + 1) mine = nb;
         }
         if (V & 1) {
-            const float na = eval_one<W>(D, pw, slots, lane, V - 1, d);
+            const float na = eval_one<W, HW>(D, pw, slots, lane, V - 1, d);
             if (lane == V - 1) mine = na;
         }
         if (lane < V) D.cost[(size_t)p * V + lane] = mine;
@@ -295,7 +295,7 @@ __global__ void __launch_bounds__(COST_BLOCK) costs_kernel(const RefDesc *refs, 
 }
 
 // Windowed NCC for a list of queries, one warp per query.
-template <int W>
+template <int W, bool HW>
 __global__ void __launch_bounds__(COST_BLOCK) eval_kernel(const RefDesc *refs, int r, int n,
                                                           const int4 *q, const float *depths,
                                                           float *out)
@@ -313,7 +313,7 @@ __global__ void __launch_bounds__(COST_BLOCK) eval_kernel(const RefDesc *refs, i
         const int4 t = q[i];  // x, y, view, axis
         PixelWindow<W> pw;
         load_window<W>(D, t.x, t.y, t.w, lane, slots, btab, pw);
-        const float v = eval_one<W>(D, pw, slots, lane, t.z, depths[i]);
+        const float v = eval_one<W, HW>(D, pw, slots, lane, t.z, depths[i]);
         if (lane == 0) out[i] = v;
     }
 }

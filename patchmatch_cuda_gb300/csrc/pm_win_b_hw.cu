@@ -1,0 +1,5 @@
+// Window sides 13..17 of the window-templated kernels, texture-filtering sampler.
+#define PM_GROUP_FN launch_group_b_hw
+#define PM_HW true
+#define PM_WINDOW_LIST(X) X(13) X(15) X(17)
+#include "pm_windows.inc"
