@@ -44,7 +44,8 @@ typedef enum pm_status {
     PM_ERR_IO = 9,
     PM_ERR_NO_DEVICE = 10,
     PM_ERR_STATE = 11,           /* call out of order (e.g. view selection before a run)  */
-    PM_ERR_UNSUPPORTED = 12
+    PM_ERR_UNSUPPORTED = 12,
+    PM_ERR_SCRATCH_LIMIT = 13    /* image too wide for pm_box_moments_noalloc's fixed scratch */
 } pm_status;
 
 #define PM_MAX_SOURCE_VIEWS 32
@@ -198,6 +199,26 @@ pm_status pm_sample_source(pm_handle *h, int view, int n, const float *xs, const
 pm_status pm_transpose_layers(const float *d_in, size_t in_pitch, float *d_out,
                               size_t out_pitch, int width, int height, int layers,
                               void *stream);
+
+/* ---- reference-window moments without any device allocation -----------------------------
+ * No counterpart in the reference: an addition for callers that cannot allocate device
+ * memory (work recorded inside a stream capture that must not gain allocation nodes, hosts
+ * whose framework owns every allocation, plugins that may only use the buffers they are
+ * given). Same results as the box sums of pm_create's preparation (array2d_refImg.cu:11-67,
+ * summed in double): for every pixel of a width x height float image in DEVICE memory, the
+ * window sums S_I and S_II over the (2 half_window + 1)^2 window with zero border, and
+ * c1 = S_II - S_I^2 / n over its n in-bounds pixels, clamped to 0 below 1e-5. Any output
+ * pointer may be NULL. Intermediate row sums live in a fixed scratch array inside the library
+ * (PM_NOALLOC_SCRATCH_DOUBLES doubles, 8 MiB, held on every device that loads the library
+ * until the process exits); the image is processed in row strips that fit it, and a width
+ * for which two rows plus the window's margin do not fit returns PM_ERR_SCRATCH_LIMIT. The
+ * first call on a device resolves the scratch address (make it before any stream capture).
+ * All calls on a device share the scratch: calls that overlap on the GPU race. Nothing is
+ * allocated and the work is enqueued on `stream` (NULL: the default stream). */
+#define PM_NOALLOC_SCRATCH_DOUBLES (1u << 20)
+pm_status pm_box_moments_noalloc(const float *d_ref, size_t ref_pitch, int width, int height,
+                                 int half_window, float *d_sum_i, float *d_sum_ii, float *d_c1,
+                                 size_t out_pitch, void *stream);
 
 /* ---- Philox draws (array2d_psng replacement) -------------------------------------------
  * Device-side Philox4x32-10 for n counters; out gets 4 words per counter. */

@@ -17,7 +17,7 @@ STATUS_NAMES = {
     0: "PM_OK", 1: "PM_ERR_INVALID_ARGUMENT", 2: "PM_ERR_WINDOW_SIZE", 3: "PM_ERR_TOO_FEW_VIEWS",
     4: "PM_ERR_TOO_MANY_VIEWS", 5: "PM_ERR_IMAGE", 6: "PM_ERR_CAMERA", 7: "PM_ERR_CUDA",
     8: "PM_ERR_OUT_OF_MEMORY", 9: "PM_ERR_IO", 10: "PM_ERR_NO_DEVICE", 11: "PM_ERR_STATE",
-    12: "PM_ERR_UNSUPPORTED",
+    12: "PM_ERR_UNSUPPORTED", 13: "PM_ERR_SCRATCH_LIMIT",
 }
 
 PREFILTER_NONE, PREFILTER_BOX, PREFILTER_GAUSSIAN = 0, 1, 2
@@ -33,7 +33,7 @@ EXPORTED_SYMBOLS = [
     "pm_save_depth", "pm_get_stats", "pm_get_stream", "pm_get_size", "pm_init_depth",
     "pm_compute_costs", "pm_run_sweep", "pm_set_depth", "pm_get_costs", "pm_set_costs",
     "pm_get_ref_maps", "pm_get_source_texels", "pm_eval_costs", "pm_sample_source",
-    "pm_transpose_layers", "pm_philox",
+    "pm_transpose_layers", "pm_philox", "pm_box_moments_noalloc",
 ]
 
 
@@ -111,6 +111,7 @@ def load_engine() -> C.CDLL:
         "pm_sample_source": (C.c_int, [H, C.c_int, C.c_int, P, P, P]),
         "pm_transpose_layers": (C.c_int, [P, C.c_size_t, P, C.c_size_t, C.c_int, C.c_int, C.c_int, P]),
         "pm_philox": (C.c_int, [C.c_uint64, C.c_int, P, P]),
+        "pm_box_moments_noalloc": (C.c_int, [P, C.c_size_t, C.c_int, C.c_int, C.c_int, P, P, P, C.c_size_t, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -51,7 +51,8 @@ namespace {
 const char *kStatusStrings[] = {
     "ok", "invalid argument", "window size out of range", "too few views",
     "too many source views", "invalid image", "invalid camera", "CUDA error", "out of memory",
-    "I/O error", "no CUDA device", "call out of order", "unsupported"};
+    "I/O error", "no CUDA device", "call out of order", "unsupported",
+    "image too wide for the fixed scratch of pm_box_moments_noalloc"};
 
 pm_status fail(pm_handle *h, pm_status s, const std::string &msg)
 {
