@@ -172,8 +172,8 @@ class Oracle:
         self.sum_ii = np.ascontiguousarray(sum_ii, np.float64)
 
     def sample(self, view, xs, ys) -> np.ndarray:
-        xs = np.ascontiguousarray(xs, np.float32)
-        ys = np.ascontiguousarray(ys, np.float32)
+        xs = np.ascontiguousarray(xs, np.float32).ravel()
+        ys = np.ascontiguousarray(np.broadcast_to(ys, xs.shape), np.float32)
         out = np.empty(xs.shape, np.float64)
         self.lib.pmo_sample(self._pp, view, xs.size, xs.ctypes.data, ys.ctypes.data, out.ctypes.data)
         return out
@@ -182,10 +182,10 @@ class Oracle:
         return self.lib.pmo_ncc(self._pp, self.sum_i.ctypes.data, self.sum_ii.ctypes.data, x, y, view, depth, axis)
 
     def ncc_batch(self, xs, ys, views, depths, axes) -> np.ndarray:
-        xs = np.ascontiguousarray(xs, np.int32)
-        ys = np.ascontiguousarray(ys, np.int32)
-        vs = np.ascontiguousarray(views, np.int32)
-        ds = np.ascontiguousarray(depths, np.float64)
+        xs = np.ascontiguousarray(xs, np.int32).ravel()
+        ys = np.ascontiguousarray(np.broadcast_to(ys, xs.shape), np.int32)
+        vs = np.ascontiguousarray(np.broadcast_to(views, xs.shape), np.int32)
+        ds = np.ascontiguousarray(np.broadcast_to(depths, xs.shape), np.float64)
         ax = np.ascontiguousarray(np.broadcast_to(axes, xs.shape), np.int32)
         out = np.empty(xs.shape, np.float64)
         self.lib.pmo_ncc_batch(self._pp, self.sum_i.ctypes.data, self.sum_ii.ctypes.data, xs.size, xs.ctypes.data,

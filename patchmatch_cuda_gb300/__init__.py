@@ -245,10 +245,10 @@ class Engine:
         return out
 
     def eval_costs(self, xs, ys, views, depths, axes) -> np.ndarray:
-        xs = np.ascontiguousarray(xs, np.int32)
-        ys = np.ascontiguousarray(ys, np.int32)
-        vs = np.ascontiguousarray(views, np.int32)
-        ds = np.ascontiguousarray(depths, np.float32)
+        xs = np.ascontiguousarray(xs, np.int32).ravel()
+        ys = np.ascontiguousarray(np.broadcast_to(ys, xs.shape), np.int32)
+        vs = np.ascontiguousarray(np.broadcast_to(views, xs.shape), np.int32)
+        ds = np.ascontiguousarray(np.broadcast_to(depths, xs.shape), np.float32)
         ax = np.ascontiguousarray(np.broadcast_to(axes, xs.shape), np.int32)
         out = np.empty(xs.shape, np.float32)
         self._chk(self._lib.pm_eval_costs(self.h, xs.size, xs.ctypes.data, ys.ctypes.data, vs.ctypes.data,
@@ -256,8 +256,8 @@ class Engine:
         return out
 
     def sample_source(self, view: int, xs, ys) -> np.ndarray:
-        xs = np.ascontiguousarray(xs, np.float32)
-        ys = np.ascontiguousarray(ys, np.float32)
+        xs = np.ascontiguousarray(xs, np.float32).ravel()
+        ys = np.ascontiguousarray(np.broadcast_to(ys, xs.shape), np.float32)
         out = np.empty(xs.shape, np.float32)
         self._chk(self._lib.pm_sample_source(self.h, view, xs.size, xs.ctypes.data, ys.ctypes.data,
                                              out.ctypes.data))

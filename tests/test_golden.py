@@ -1,0 +1,57 @@
+"""Committed golden vectors (tests/golden/plane3_128x96.npz, written by make_golden.py from the
+FP64 oracle): the oracle must still reproduce them (CPU), and the engine must match them (GPU)."""
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+sys.path.insert(0, str(GOLDEN))
+import make_golden  # noqa: E402
+
+
+@pytest.fixture(scope="module")
+def golden():
+    z = np.load(GOLDEN / "plane3_128x96.npz")
+    return {k: z[k] for k in z.files}
+
+
+def _images(g):
+    from patchmatch_cuda_gb300 import Image
+    return [Image(g["K"][i], g["R"][i], g["T"][i], g["images"][i]) for i in range(len(g["images"]))]
+
+
+def test_oracle_reproduces_golden(oracle_lib, golden):
+    from patchmatch_cuda_gb300.scene import SceneViews
+    sv = SceneViews(_images(golden), int(golden["ref_id"]), golden["gt_depth"], make_golden.WORKLOAD)
+    got = make_golden.compute(sv)
+    for k in ("init_depth", "init_costs", "depth", "view_sel"):
+        np.testing.assert_array_equal(got[k], golden[k], err_msg=k)
+    np.testing.assert_allclose(got["ncc"], golden["ncc"], rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.gpu
+def test_engine_matches_golden(golden, parity_log):
+    from patchmatch_cuda_gb300 import Engine
+    w = make_golden.WORKLOAD
+    eng = Engine(_images(golden), int(golden["ref_id"]), w.params())
+    xs, ys, vs, ds, ax = make_golden.queries()
+    got = eng.eval_costs(xs, ys, vs, ds, ax)
+    want = golden["ncc"]
+    err = np.abs(got - want) / np.maximum(1.0, np.abs(want))
+    eng.init_depth()
+    np.testing.assert_allclose(eng.depth(), golden["init_depth"], rtol=2e-7, atol=1e-6)
+    eng.set_depth(golden["init_depth"])
+    eng.compute_costs(1)
+    c = eng.costs()
+    cerr = np.abs(c - golden["init_costs"]) / np.maximum(1.0, np.abs(golden["init_costs"]))
+    eng.run()
+    depth = eng.depth()
+    rel = np.abs(depth - golden["depth"]) / golden["depth"]
+    parity_log("golden_plane3_128x96", ncc_err_max=float(err.max()), init_cost_err_max=float(cerr.max()),
+               depth_within_0p1pct=float(np.mean(rel <= 1e-3)))
+    assert err.max() <= 1e-4
+    assert cerr.max() <= 1e-4
+    assert np.mean(rel <= 1e-3) >= 0.99
+    eng.close()
