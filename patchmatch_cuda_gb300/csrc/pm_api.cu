@@ -37,6 +37,9 @@ struct pm_handle {
     RefDesc h_desc{};
     cudaArray_t arr[MAX_VIEWS] = {};
     cudaTextureObject_t tex[MAX_VIEWS] = {};
+    cudaArray_t layered = nullptr;          // texture-filtering sampler: sources as layers
+    cudaTextureObject_t tex_layered = 0;
+    int layer_w = 0, layer_h = 0;
     int src_w[MAX_VIEWS] = {}, src_h[MAX_VIEWS] = {};
     SweepArgs *h_sweep_args = nullptr;   // pinned, one per sweep of the schedule
 
@@ -155,19 +158,19 @@ int prefilter_taps(int mode, float sigma, float *w)
 
 // ---- a small cache of gather-capable CUDA arrays, so handle churn does not reallocate ----
 struct ArrayKey {
-    int device, w, h, bytes;
+    int device, w, h, bytes, layers;  // layers 0: a plain 2-D gather array
 };
 std::mutex g_array_mutex;
 std::vector<std::pair<ArrayKey, cudaArray_t>> g_free_arrays;
 bool g_pool_ready[64] = {};
 
-cudaError_t acquire_array(int device, int w, int h, int bytes, cudaArray_t *out)
+cudaError_t acquire_array(int device, int w, int h, int bytes, cudaArray_t *out, int layers = 0)
 {
     {
         std::lock_guard<std::mutex> lk(g_array_mutex);
         for (size_t i = 0; i < g_free_arrays.size(); ++i) {
             const ArrayKey &k = g_free_arrays[i].first;
-            if (k.device == device && k.w == w && k.h == h && k.bytes == bytes) {
+            if (k.device == device && k.w == w && k.h == h && k.bytes == bytes && k.layers == layers) {
                 *out = g_free_arrays[i].second;
                 g_free_arrays.erase(g_free_arrays.begin() + (long)i);
                 return cudaSuccess;
@@ -177,13 +180,16 @@ cudaError_t acquire_array(int device, int w, int h, int bytes, cudaArray_t *out)
     cudaChannelFormatDesc fmt = bytes == 1   ? cudaCreateChannelDesc<unsigned char>()
                                 : bytes == 2 ? cudaCreateChannelDescHalf()
                                              : cudaCreateChannelDesc<float>();
+    if (layers > 0)
+        return cudaMalloc3DArray(out, &fmt, make_cudaExtent((size_t)w, (size_t)h, (size_t)layers),
+                                 cudaArrayLayered);
     return cudaMallocArray(out, &fmt, (size_t)w, (size_t)h, cudaArrayTextureGather);
 }
 
-void release_array(int device, int w, int h, int bytes, cudaArray_t a)
+void release_array(int device, int w, int h, int bytes, cudaArray_t a, int layers = 0)
 {
     std::lock_guard<std::mutex> lk(g_array_mutex);
-    if (g_free_arrays.size() < 256) g_free_arrays.push_back({ArrayKey{device, w, h, bytes}, a});
+    if (g_free_arrays.size() < 256) g_free_arrays.push_back({ArrayKey{device, w, h, bytes, layers}, a});
     else cudaFreeArray(a);
 }
 
@@ -423,6 +429,8 @@ pm_status pm_destroy(pm_handle *h)
         if (h->tex[v]) cudaDestroyTextureObject(h->tex[v]);
         if (h->arr[v]) release_array(h->device, h->src_w[v], h->src_h[v], h->texel_bytes, h->arr[v]);
     }
+    if (h->tex_layered) cudaDestroyTextureObject(h->tex_layered);
+    if (h->layered) release_array(h->device, h->layer_w, h->layer_h, h->texel_bytes, h->layered, h->V);
     void *bufs[] = {h->d_ref, h->d_sum_i, h->d_sum_ii, h->d_c1, h->d_depth, h->d_cost, h->d_beta,
                     h->d_view_sel, h->d_evals, h->d_hh, h->d_hh64, h->d_desc};
     for (void *b : bufs)
@@ -557,6 +565,15 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
         max_h = std::max(max_h, views[i].height);
     }
     const size_t max_pix = (size_t)max_w * max_h;
+    int src_max_w = 0, src_max_h = 0;
+    for (int i = 0; i < n_views; ++i) {
+        if (i == ref_id) continue;
+        src_max_w = std::max(src_max_w, views[i].width);
+        src_max_h = std::max(src_max_h, views[i].height);
+    }
+    void *d_layer = nullptr;
+    if (p.sampler == PM_SAMPLER_HARDWARE)
+        PM_TRY(dalloc((uint8_t **)&d_layer, (size_t)src_max_w * src_max_h * h->texel_bytes, s));
     uint8_t *d_u8 = nullptr;
     float *d_f0 = nullptr, *d_f1 = nullptr, *d_f2 = nullptr;
     double *d_row_i = nullptr, *d_row_ii = nullptr;
@@ -586,34 +603,70 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
                                       h->d_c1, v.width, v.height, p.half_window, s));
             continue;
         }
+        // source texels in the array's format
+        const void *src_texels = d_u8;
+        size_t src_pitch = (size_t)v.width;
+        if (h->texel_bytes == 2) {
+            PM_TRY(launch_float_to_half(texels, d_f2, v.width * v.height, s));
+            src_texels = d_f2;
+            src_pitch = (size_t)v.width * 2;
+        } else if (h->texel_bytes == 4) {
+            src_texels = texels;
+            src_pitch = (size_t)v.width * 4;
+        }
+        if (p.sampler == PM_SAMPLER_HARDWARE) {
+            // one layer per source, zero-padded to the largest source (the reference's layout,
+            // patchMatch.cu:72-95); the padding reads as the border's zero
+            if (!h->layered) {
+                h->layer_w = src_max_w;
+                h->layer_h = src_max_h;
+                PM_TRY(acquire_array(device, h->layer_w, h->layer_h, h->texel_bytes, &h->layered, h->V));
+            }
+            const size_t lp = (size_t)h->layer_w * h->texel_bytes;
+            PM_TRY(cudaMemsetAsync(d_layer, 0, lp * h->layer_h, s));
+            PM_TRY(cudaMemcpy2DAsync(d_layer, lp, src_texels, src_pitch, src_pitch, (size_t)v.height,
+                                     cudaMemcpyDeviceToDevice, s));
+            cudaMemcpy3DParms cp{};
+            cp.srcPtr = make_cudaPitchedPtr(d_layer, lp, (size_t)h->layer_w, (size_t)h->layer_h);
+            cp.dstArray = h->layered;
+            cp.dstPos = make_cudaPos(0, 0, (size_t)si);
+            cp.extent = make_cudaExtent((size_t)h->layer_w, (size_t)h->layer_h, 1);
+            cp.kind = cudaMemcpyDeviceToDevice;
+            PM_TRY(cudaMemcpy3DAsync(&cp, s));
+            ++si;
+            continue;
+        }
         cudaArray_t arr = nullptr;
         PM_TRY(acquire_array(device, v.width, v.height, h->texel_bytes, &arr));
         h->arr[si] = arr;
-        if (h->texel_bytes == 1) {
-            PM_TRY(cudaMemcpy2DToArrayAsync(arr, 0, 0, d_u8, (size_t)v.width, (size_t)v.width,
-                                            (size_t)v.height, cudaMemcpyDeviceToDevice, s));
-        } else if (h->texel_bytes == 2) {
-            PM_TRY(launch_float_to_half(texels, d_f2, v.width * v.height, s));
-            PM_TRY(cudaMemcpy2DToArrayAsync(arr, 0, 0, d_f2, (size_t)v.width * 2,
-                                            (size_t)v.width * 2, (size_t)v.height,
-                                            cudaMemcpyDeviceToDevice, s));
-        } else {
-            PM_TRY(cudaMemcpy2DToArrayAsync(arr, 0, 0, texels, (size_t)v.width * 4,
-                                            (size_t)v.width * 4, (size_t)v.height,
-                                            cudaMemcpyDeviceToDevice, s));
-        }
+        PM_TRY(cudaMemcpy2DToArrayAsync(arr, 0, 0, src_texels, src_pitch, src_pitch, (size_t)v.height,
+                                        cudaMemcpyDeviceToDevice, s));
         cudaResourceDesc rd{};
         rd.resType = cudaResourceTypeArray;
         rd.res.array.array = arr;
         cudaTextureDesc td{};
         td.addressMode[0] = cudaAddressModeBorder;
         td.addressMode[1] = cudaAddressModeBorder;
-        td.filterMode = p.sampler == PM_SAMPLER_HARDWARE ? cudaFilterModeLinear : cudaFilterModePoint;
+        td.filterMode = cudaFilterModePoint;
         td.readMode = h->texel_bytes == 1 ? cudaReadModeNormalizedFloat : cudaReadModeElementType;
         td.normalizedCoords = 0;
         PM_TRY(cudaCreateTextureObject(&h->tex[si], &rd, &td, nullptr));
         ++si;
     }
+    if (p.sampler == PM_SAMPLER_HARDWARE) {
+        cudaResourceDesc rd{};
+        rd.resType = cudaResourceTypeArray;
+        rd.res.array.array = h->layered;
+        cudaTextureDesc td{};
+        td.addressMode[0] = cudaAddressModeBorder;
+        td.addressMode[1] = cudaAddressModeBorder;
+        td.addressMode[2] = cudaAddressModeBorder;
+        td.filterMode = cudaFilterModeLinear;
+        td.readMode = h->texel_bytes == 1 ? cudaReadModeNormalizedFloat : cudaReadModeElementType;
+        td.normalizedCoords = 0;
+        PM_TRY(cudaCreateTextureObject(&h->tex_layered, &rd, &td, nullptr));
+    }
+    if (d_layer) PM_TRY(cudaFreeAsync(d_layer, s));
     PM_TRY(cudaFreeAsync(d_u8, s));
     PM_TRY(cudaFreeAsync(d_f0, s));
     PM_TRY(cudaFreeAsync(d_f1, s));
@@ -650,6 +703,7 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
     D.evals = h->d_evals;
     D.hh = h->d_hh;
     D.hh64 = h->d_hh64;
+    D.tex_layered = h->tex_layered;
     for (int v = 0; v < h->V; ++v) {
         D.tex[v] = h->tex[v];
         D.src_w[v] = (float)h->src_w[v];
@@ -952,8 +1006,19 @@ pm_status pm_get_source_texels(pm_handle *h, int view, float *dst)
     if (st != PM_OK) return st;
     const int w = h->src_w[view], hgt = h->src_h[view], b = h->texel_bytes;
     std::vector<uint8_t> raw((size_t)w * hgt * b);
-    PM_CUDA(h, cudaMemcpy2DFromArrayAsync(raw.data(), (size_t)w * b, h->arr[view], 0, 0,
-                                          (size_t)w * b, (size_t)hgt, cudaMemcpyDeviceToHost, h->stream));
+    if (h->layered) {
+        cudaMemcpy3DParms cp{};
+        cp.srcArray = h->layered;
+        cp.srcPos = make_cudaPos(0, 0, (size_t)view);
+        cp.dstPtr = make_cudaPitchedPtr(raw.data(), (size_t)w * b, (size_t)w, (size_t)hgt);
+        cp.extent = make_cudaExtent((size_t)w, (size_t)hgt, 1);
+        cp.kind = cudaMemcpyDeviceToHost;
+        PM_CUDA(h, cudaMemcpy3DAsync(&cp, h->stream));
+    } else {
+        PM_CUDA(h, cudaMemcpy2DFromArrayAsync(raw.data(), (size_t)w * b, h->arr[view], 0, 0,
+                                              (size_t)w * b, (size_t)hgt, cudaMemcpyDeviceToHost,
+                                              h->stream));
+    }
     PM_CUDA(h, cudaStreamSynchronize(h->stream));
     const size_t n = (size_t)w * hgt;
     if (b == 1) {

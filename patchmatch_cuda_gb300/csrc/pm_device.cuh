@@ -51,6 +51,7 @@ struct RefDesc {
     unsigned long long *evals;      // [0] algorithmic count, [1] computed count
     const float4 *hh;               // n_src * 5 float4: H1 (9), H2 (9), pad (2)
     const double *hh64;             // n_src * 18 (mixed precision window origin)
+    cudaTextureObject_t tex_layered;  // all sources as layers (texture-filtering sampler)
     cudaTextureObject_t tex[MAX_VIEWS];
     float src_w[MAX_VIEWS], src_h[MAX_VIEWS];
 };
@@ -96,11 +97,29 @@ __device__ __forceinline__ float sample_source(cudaTextureObject_t tex, float xs
     return fmaf(ay, bot - top, top);
 }
 
-// Texture-unit bilinear filtering at source coordinate (xs, ys) (texel i at i): the fetch of
-// patchMatch.cu:543 itself, with the hardware's fixed-point weights.
-__device__ __forceinline__ float sample_source_hw(cudaTextureObject_t tex, float xs, float ys)
+// Texture-unit bilinear filtering at source coordinate (xs, ys) (texel i at i) of layer `view`:
+// the fetch of patchMatch.cu:543 itself, with the hardware's fixed-point weights. All sources
+// share one layered texture (zero-padded to the largest view), so the texture handle is the
+// same for every lane.
+__device__ __forceinline__ float sample_source_hw(cudaTextureObject_t tex, int view, float xs, float ys)
 {
-    return tex2D<float>(tex, xs + 0.5f, ys + 0.5f);
+    return tex2DLayered<float>(tex, xs + 0.5f, ys + 0.5f, view);
+}
+
+// The same fetch without a branch: coordinates are clamped to a safe finite range (NaN maps to
+// the low end), the gather always runs, and out-of-range results are replaced by 0 afterwards.
+__device__ __forceinline__ float sample_source_nb(cudaTextureObject_t tex, float xs, float ys,
+                                                  float sw, float sh)
+{
+    const bool in = xs > -1.0f && xs < sw && ys > -1.0f && ys < sh;
+    const float xc = fminf(fmaxf(xs, -2.0f), sw + 1.0f);
+    const float yc = fminf(fmaxf(ys, -2.0f), sh + 1.0f);
+    const float fx = floorf(xc), fy = floorf(yc);
+    const float ax = xc - fx, ay = yc - fy;
+    const float4 g = tex2Dgather<float4>(tex, fx + 1.0f, fy + 1.0f, 0);
+    const float top = fmaf(ax, g.z - g.w, g.w);
+    const float bot = fmaf(ax, g.y - g.x, g.x);
+    return in ? fmaf(ay, bot - top, top) : 0.0f;
 }
 
 __device__ __forceinline__ float warp_sum(float v)
@@ -270,8 +289,8 @@ __device__ __forceinline__ WarpSetup warp_setup(const RefDesc &D, int view, floa
 }
 
 template <bool HW>
-__device__ __forceinline__ float warp_sample(const WarpSetup &A, cudaTextureObject_t tex, float sw,
-                                             float sh, float dx, float dy)
+__device__ __forceinline__ float warp_sample(const WarpSetup &A, cudaTextureObject_t tex, int layer,
+                                             float sw, float sh, float dx, float dy)
 {
     const float px = fmaf(A.c0x, dx, fmaf(A.c1x, dy, A.bx));
     const float py = fmaf(A.c0y, dx, fmaf(A.c1y, dy, A.by));
@@ -281,10 +300,10 @@ __device__ __forceinline__ float warp_sample(const WarpSetup &A, cudaTextureObje
         // px, py already carry the texture's half-texel offset
         pz = fabsf(pz) < 1e-20f ? 1e-20f : pz;
         const float r = __fdividef(1.0f, pz);
-        return tex2D<float>(tex, px * r, py * r);
+        return tex2DLayered<float>(tex, px * r, py * r, layer);
     }
     const float r = __fdividef(1.0f, pz);
-    return sample_source(tex, px * r, py * r, sw, sh);
+    return sample_source_nb(tex, px * r, py * r, sw, sh);
 }
 
 // Whether lane `lane`'s slot i is a window sample: the window may not fill the last slot.
@@ -303,13 +322,14 @@ __device__ __forceinline__ void eval_core(const RefDesc &D, const PixelWindow<W>
                                           const float (&d)[E], float (&out)[E])
 {
     constexpr int NS = Window<W>::NS;
+    constexpr int LAST_LANES = Window<W>::NSAMP - 32 * (NS - 1);  // lanes holding the last slot
     WarpSetup A[E];
     cudaTextureObject_t tex[E];
     float sw[E], sh[E];
 #pragma unroll
     for (int e = 0; e < E; ++e) {
         A[e] = warp_setup<HW>(D, v[e], d[e], pw.scale, pw.ox, pw.oy);
-        tex[e] = D.tex[v[e]];
+        tex[e] = HW ? D.tex_layered : D.tex[v[e]];
         sw[e] = D.src_w[v[e]];
         sh[e] = D.src_h[v[e]];
     }
@@ -319,15 +339,22 @@ __device__ __forceinline__ void eval_core(const RefDesc &D, const PixelWindow<W>
     for (int e = 0; e < E; ++e) j[e] = 0.f;
 #pragma unroll
     for (int i = 0; i < NS; ++i) {
-        const bool take = FULL ? slot_exists<W>(i, lane) : ((pw.inb >> i) & 1) != 0;
         const float2 o = slots[32 * i + lane];
+        // Interior windows sample every full slot unconditionally (no branch between the
+        // fetches, so they can all be in flight at once); the partially filled last slot and
+        // windows cut by the image border keep a per-slot test.
+        const bool guarded = !FULL || (i == NS - 1 && LAST_LANES < 32);
+        const bool take = FULL ? (i < NS - 1 || lane < LAST_LANES) : ((pw.inb >> i) & 1) != 0;
 #pragma unroll
         for (int e = 0; e < E; ++e) {
-            smp[e][i] = 0.f;
-            if (take) {
-                smp[e][i] = warp_sample<HW>(A[e], tex[e], sw[e], sh[e], o.x, o.y);
-                j[e] += smp[e][i];
+            float sv = 0.f;
+            if (guarded) {
+                if (take) sv = warp_sample<HW>(A[e], tex[e], v[e], sw[e], sh[e], o.x, o.y);
+            } else {
+                sv = warp_sample<HW>(A[e], tex[e], v[e], sw[e], sh[e], o.x, o.y);
             }
+            smp[e][i] = sv;
+            j[e] += sv;
         }
     }
     float m[E], q[E], x[E];
@@ -340,15 +367,13 @@ __device__ __forceinline__ void eval_core(const RefDesc &D, const PixelWindow<W>
     }
 #pragma unroll
     for (int i = 0; i < NS; ++i) {
-        const bool take = FULL ? slot_exists<W>(i, lane) : ((pw.inb >> i) & 1) != 0;
-        if (take) {
-            const float bi = pw.b[32 * i + lane];
+        const bool take = FULL ? (i < NS - 1 || lane < LAST_LANES) : ((pw.inb >> i) & 1) != 0;
+        const float bi = pw.b[32 * i + lane];
 #pragma unroll
-            for (int e = 0; e < E; ++e) {
-                const float de = smp[e][i] - m[e];
-                q[e] = fmaf(de, de, q[e]);
-                x[e] = fmaf(de, bi, x[e]);
-            }
+        for (int e = 0; e < E; ++e) {
+            const float de = take ? smp[e][i] - m[e] : 0.0f;
+            q[e] = fmaf(de, de, q[e]);
+            x[e] = fmaf(de, bi, x[e]);
         }
     }
 #pragma unroll
@@ -366,7 +391,8 @@ __device__ __forceinline__ float eval_one(const RefDesc &D, const PixelWindow<W>
     const int vv[1] = {v};
     const float dd[1] = {d};
     float out[1];
-    eval_core<W, 1, HW, false>(D, pw, slots, lane, vv, dd, out);
+    if (pw.full) eval_core<W, 1, HW, true>(D, pw, slots, lane, vv, dd, out);
+    else eval_core<W, 1, HW, false>(D, pw, slots, lane, vv, dd, out);
     return out[0];
 }
 
@@ -378,7 +404,8 @@ __device__ __forceinline__ void eval_pair(const RefDesc &D, const PixelWindow<W>
     const int vv[2] = {va, vb};
     const float dd[2] = {da, db};
     float out[2];
-    eval_core<W, 2, HW, false>(D, pw, slots, lane, vv, dd, out);
+    if (pw.full) eval_core<W, 2, HW, true>(D, pw, slots, lane, vv, dd, out);
+    else eval_core<W, 2, HW, false>(D, pw, slots, lane, vv, dd, out);
     out_a = out[0];
     out_b = out[1];
 }

@@ -103,7 +103,7 @@ __global__ void sample_kernel(const RefDesc *refs, int r, int view, int n,
     const RefDesc &D = refs[r];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n)
-        out[i] = D.hw_filter ? sample_source_hw(D.tex[view], xs[i], ys[i])
+        out[i] = D.hw_filter ? sample_source_hw(D.tex_layered, view, xs[i], ys[i])
                              : sample_source(D.tex[view], xs[i], ys[i], D.src_w[view], D.src_h[view]);
 }
 
