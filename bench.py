@@ -348,6 +348,18 @@ def run_ours(args):
     e2e_value = total_evals / e2e_max / 1e9
 
     tpl = eng.stats().threads_per_line
+    # variants of the same workload, each one depth map timed once after a warm-up run
+    variants = {}
+    for name, over in [("f32_texels_box_prefilter", dict(prefilter=1)),
+                       ("f16_texels_box_prefilter", dict(prefilter=1, precision=1)),
+                       ("exact_sampler", dict(sampler=0))]:
+        ev = Engine(sv.images, sv.ref_id, wl.params(gpu_id=local, **over))
+        ev.run()
+        ev.run()
+        st = ev.stats()
+        variants[name] = {"ms_per_depth_map": st.ms_total, "g_cost_evals_per_s": st.cost_evals / st.ms_total / 1e6,
+                          "bad_pixel_pct_1pct": round(100 * scene.bad_pixel_rate(ev.depth(), sv.gt_depth), 3)}
+        ev.close()
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(eng, sv, wl, args.cpu_seconds)
@@ -359,12 +371,16 @@ def run_ours(args):
             "metric": "G cost-evals/s", "value": total_evals / (total_ms * 1e-3) / 1e9, "unit": "G cost-evals/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32" if args.precision == 0 else "f16 texels, f32 moments",
-            "data": "synthetic (seeded scene: 12 planes + 200 boxes, 1 ref + 10 sources on a 15 degree arc)",
+            "vs_baseline": None,
+            "dtype": ("u8 texels, f32 arithmetic" if wl.prefilter == 0 else "f32") if args.precision == 0
+            else "f16 texels, f32 arithmetic",
+            "data": f"synthetic (seeded scene: {wl.n_planes} planes + {wl.n_boxes} boxes, 1 ref + {wl.n_src} sources on a 15 degree arc)",
             "config": {
                 "workload": args.workload, "width": wl.width, "height": wl.height, "n_src": wl.n_src,
                 "window": w, "iterations": wl.iterations, "num_samples": wl.num_samples,
-                "prefilter": "box, sigma 1", "precision": "fp32" if args.precision == 0 else "mixed",
+                "prefilter": "none" if wl.prefilter == 0 else "box, sigma 1",
+                "precision": "fp32" if args.precision == 0 else "mixed",
+                "sampler": "texture-unit bilinear (the reference's fetch)" if params.sampler == 1 else "exact gather",
                 "ms_per_depth_map": total_ms / args.steps, "cost_evals_per_depth_map": evals_per_map,
                 "bad_pixel_pct_1pct": round(100 * bad, 3),
                 "l2": "flushed before each depth map (256 MiB write, outside the timed events)",
@@ -382,6 +398,7 @@ def run_ours(args):
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "G cost-evals/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_max / args.steps},
+            "variants": variants,
             "gpu_launches": launches_per_map * args.steps,
             "clocks": clocks.summary(),
         }

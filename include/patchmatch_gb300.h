@@ -63,9 +63,11 @@ typedef enum pm_precision {
 } pm_precision;
 
 typedef enum pm_sampler {
-    PM_SAMPLER_EXACT = 0,       /* 4-texel gather, exact FP32 bilinear weights              */
-    PM_SAMPLER_HARDWARE = 1     /* texture-unit bilinear filtering, 8-bit fixed-point weights
-                                   (what the reference's tex2DLayered fetch does)           */
+    PM_SAMPLER_EXACT = 0,       /* 4-texel gather, exact FP32 bilinear weights (NCC within
+                                   1e-4 of an FP64 oracle; slower)                          */
+    PM_SAMPLER_HARDWARE = 1     /* default: texture-unit bilinear filtering with 8-bit
+                                   fixed-point weights, what the reference's tex2DLayered
+                                   fetch does; FP16 texels fall back to the exact sampler   */
 } pm_sampler;
 
 typedef enum pm_texel_format {

@@ -405,6 +405,7 @@ void pm_default_params(pm_params *p)
     p->init_mode = PM_INIT_RANDOM;
     p->threads_per_line = 0;
     p->quirks = 1;
+    p->sampler = PM_SAMPLER_HARDWARE;
     p->gpu_id = -1;
     p->block_dim_x = 32;
     p->block_dim_y = 16;
@@ -498,6 +499,8 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
     const bool filtered = p.prefilter != PM_PREFILTER_NONE;
     h->texel_bytes = p.texel_format != PM_TEXELS_AUTO ? p.texel_format
                      : p.precision == PM_PRECISION_FP32 ? (filtered ? 4 : 1) : (filtered ? 2 : 1);
+    // The texture unit filters FP16 texels in reduced precision (about 2e-3): gather instead.
+    if (h->texel_bytes == 2) h->p.sampler = PM_SAMPLER_EXACT;
 
     // camera setup
     double kr[9], kr_inv[9];
@@ -572,7 +575,7 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
         src_max_h = std::max(src_max_h, views[i].height);
     }
     void *d_layer = nullptr;
-    if (p.sampler == PM_SAMPLER_HARDWARE)
+    if (h->p.sampler == PM_SAMPLER_HARDWARE)
         PM_TRY(dalloc((uint8_t **)&d_layer, (size_t)src_max_w * src_max_h * h->texel_bytes, s));
     uint8_t *d_u8 = nullptr;
     float *d_f0 = nullptr, *d_f1 = nullptr, *d_f2 = nullptr;
@@ -614,7 +617,7 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
             src_texels = texels;
             src_pitch = (size_t)v.width * 4;
         }
-        if (p.sampler == PM_SAMPLER_HARDWARE) {
+        if (h->p.sampler == PM_SAMPLER_HARDWARE) {
             // one layer per source, zero-padded to the largest source (the reference's layout,
             // patchMatch.cu:72-95); the padding reads as the border's zero
             if (!h->layered) {
@@ -653,7 +656,7 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
         PM_TRY(cudaCreateTextureObject(&h->tex[si], &rd, &td, nullptr));
         ++si;
     }
-    if (p.sampler == PM_SAMPLER_HARDWARE) {
+    if (h->p.sampler == PM_SAMPLER_HARDWARE) {
         cudaResourceDesc rd{};
         rd.resType = cudaResourceTypeArray;
         rd.res.array.array = h->layered;
@@ -689,7 +692,7 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
     D.ik00 = (float)kr_inv[0];
     D.ik02 = (float)kr_inv[2];
     D.quirks = p.quirks ? 1 : 0;
-    D.hw_filter = p.sampler == PM_SAMPLER_HARDWARE ? 1 : 0;
+    D.hw_filter = h->p.sampler == PM_SAMPLER_HARDWARE ? 1 : 0;
     D.batch_id = 0;
     D.seed = p.seed;
     D.ref = h->d_ref;

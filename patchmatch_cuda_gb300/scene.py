@@ -6,7 +6,7 @@ index, the reference's ground-truth z-depth and the engine parameters.
     plane3_320x240     3 slanted planes, 1 ref + 4 sources on a 15 degree arc, f = 300 px,
                        depth [2, 8], 11x11 window, box prefilter sigma 1, 3 iterations
     box200_1280x720    12 planes + 200 boxes, 1 ref + 10 sources, depth [1, 20], 15x15 window,
-                       5 iterations
+                       5 iterations, no prefilter (the reference's runtime never calls its blur)
     batch24_mixed      24 references of 640x480 / 1280x720 / 1920x1080 with 6-12 sources each
                        from one scene of 40 planes + 500 boxes, 15x15 window, 5 iterations
     box2000_3072x2048  60 planes + 2000 boxes, 1 ref + 20 sources, depth [0.5, 50], 19x19 window
@@ -21,7 +21,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from . import Image, PREFILTER_BOX, _native
+from . import Image, PREFILTER_BOX, PREFILTER_NONE, _native
 
 ARC_DEGREES = 15.0
 
@@ -67,8 +67,10 @@ class Workload:
 
 WORKLOADS = {
     "plane3_320x240": Workload("plane3_320x240", 320, 240, 4, 5, 3, 2.0, 8.0, 3, 0, seed=11),
-    "box200_1280x720": Workload("box200_1280x720", 1280, 720, 10, 7, 5, 1.0, 20.0, 12, 200, seed=22),
-    "box2000_3072x2048": Workload("box2000_3072x2048", 3072, 2048, 20, 9, 5, 0.5, 50.0, 60, 2000, seed=55),
+    "box200_1280x720": Workload("box200_1280x720", 1280, 720, 10, 7, 5, 1.0, 20.0, 12, 200,
+                                prefilter=PREFILTER_NONE, seed=22),
+    "box2000_3072x2048": Workload("box2000_3072x2048", 3072, 2048, 20, 9, 5, 0.5, 50.0, 60, 2000,
+                                  prefilter=PREFILTER_NONE, seed=55),
 }
 
 

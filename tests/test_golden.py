@@ -35,7 +35,7 @@ def test_oracle_reproduces_golden(oracle_lib, golden):
 def test_engine_matches_golden(golden, parity_log):
     from patchmatch_cuda_gb300 import Engine
     w = make_golden.WORKLOAD
-    eng = Engine(_images(golden), int(golden["ref_id"]), w.params())
+    eng = Engine(_images(golden), int(golden["ref_id"]), w.params(sampler=0))  # the fixture's sampler
     xs, ys, vs, ds, ax = make_golden.queries()
     got = eng.eval_costs(xs, ys, vs, ds, ax)
     want = golden["ncc"]

@@ -44,7 +44,9 @@ def small_scene():
 
 
 def make_engine(sv, **over):
+    """The exact-gather sampler unless a test asks otherwise: the strict 1e-4 NCC bound."""
     from patchmatch_cuda_gb300 import Engine
+    over.setdefault("sampler", 0)
     return Engine(sv.images, sv.ref_id, sv.workload.params(**over))
 
 
@@ -242,12 +244,14 @@ def first_divergence(gd, od, direction):
     return prefix, lines.shape[1]
 
 
+@pytest.mark.parametrize("sampler", [0, 1])
 @pytest.mark.parametrize("direction", [0, 1, 2, 3])
-def test_sweep_lockstep(small_scene, direction, parity_log):
+def test_sweep_lockstep(small_scene, direction, sampler, parity_log):
     """One sweep from the same state. Decisions match until an argmin or CDF near-tie flips
     (FP32 vs FP64), after which a line legitimately diverges; such events must be rare, and
-    every cost before a line's first divergence matches to the NCC tolerance."""
-    eng = make_engine(small_scene)
+    every cost before a line's first divergence matches to the NCC tolerance (the exact
+    sampler's; the texture-filtering sampler's bound is 5x, see its NCC test)."""
+    eng = make_engine(small_scene, sampler=sampler)
     orc = oracle_for(eng, small_scene)
     eng.init_depth()
     eng.compute_costs(1)
@@ -272,17 +276,20 @@ def test_sweep_lockstep(small_scene, direction, parity_log):
         else:
             mask[steps, line] = True
     cerr = ncc_err(gc, oc)[mask]
-    parity_log(f"sweep_lockstep_dir{direction}", divergence_events=events, decisions=decisions,
+    parity_log(f"sweep_lockstep_dir{direction}_sampler{sampler}", divergence_events=events, decisions=decisions,
                divergence_rate=rate, matched_fraction=float(mask.mean()),
                cost_err_max=float(cerr.max()), cost_err_q999=float(np.quantile(cerr, 0.999)))
+    tol = NCC_TOL if sampler == 0 else 5 * NCC_TOL
     assert rate <= 2e-4, f"{events} divergences in {decisions} decisions"
-    assert cerr.max() <= NCC_TOL, f"cost error {cerr.max():.3g} before divergence"
+    assert cerr.max() <= tol, f"cost error {cerr.max():.3g} before divergence"
     eng.close()
 
 
-def test_full_run_matches_oracle(small_scene, parity_log):
+@pytest.mark.parametrize("sampler", [0, 1])
+def test_full_run_matches_oracle(small_scene, sampler, parity_log):
+    """The spec bar: at least 99.5% of final depths within 0.1% of the oracle's."""
     from patchmatch_cuda_gb300 import scene
-    eng = make_engine(small_scene)
+    eng = make_engine(small_scene, sampler=sampler)
     orc = oracle_for(eng, small_scene)
     eng.run()
     gd = eng.depth()
@@ -292,9 +299,9 @@ def test_full_run_matches_oracle(small_scene, parity_log):
     frac = float(np.mean(rel <= 1e-3))
     bad_g = scene.bad_pixel_rate(gd, small_scene.gt_depth)
     bad_o = scene.bad_pixel_rate(od.astype(np.float32), small_scene.gt_depth)
-    parity_log("full_run_plane3_320x240", within_0p1pct=frac, bad1_gpu=bad_g, bad1_oracle=bad_o)
+    parity_log(f"full_run_plane3_320x240_sampler{sampler}", within_0p1pct=frac, bad1_gpu=bad_g, bad1_oracle=bad_o)
     assert abs(bad_g - bad_o) <= 0.01, (bad_g, bad_o)
-    assert frac >= 0.95, f"only {frac:.4f} of depths within 0.1% of the oracle"
+    assert frac >= 0.995, f"only {frac:.4f} of depths within 0.1% of the oracle"
     st = eng.stats()
     assert st.cost_evals > 0
     eng.close()
