@@ -164,7 +164,7 @@ def make_batch(n_refs: int = 24, seed: int = 33, half_window: int = 7, iteration
         pitch = float(rng.uniform(-4.0, 4.0))
         f = 300.0 * w_ / 320.0
         wl = Workload(f"batch{r}", w_, h_, n_src, half_window, iterations, depth_near, depth_far,
-                      n_planes, n_boxes, seed=seed * 1000 + r)
+                      n_planes, n_boxes, prefilter=PREFILTER_NONE, seed=seed * 1000 + r)
         yaws = arc_yaws(n_src + 1, yaw_c)
         ref_id = n_src // 2
         images, gt = [], None
