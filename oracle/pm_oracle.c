@@ -88,6 +88,15 @@ static inline real draw(const pmo_problem *p, int pixel, uint32_t sweep, int pur
                              ((uint32_t)purpose << 16) | (uint32_t)sub, p->batch_id);
 }
 
+/* A depth hypothesis U * (far - near) + near as the reference forms it: in float, the span
+ * rounded to float first (array2d_wrapper.cu:15, patchMatch.cu:937), one fused multiply-add
+ * (an exact float product fits a double, so rounding the double sum once is the fused result). */
+static inline double float_depth(double u, double near, double far)
+{
+    const float span = (float)((double)(float)far - (double)(float)near);
+    return (double)(float)((double)(float)u * (double)span + (double)(float)near);
+}
+
 /* ------------------------------------------------------------------------------------
  * Camera setup: Image::updateCamParam (image.cpp:39-61: C = -R^T T, K^-1, R^-1 = R^T)
  * and Image::init_relative (image.cpp:4-13):
@@ -295,6 +304,47 @@ void pmo_sample(const pmo_problem *p, int view, int n, const float *xs, const fl
                                          (real)xs[i], (real)ys[i], p->sampler);
 }
 
+/* ------------------------------------------------------------------------------------
+ * Single-precision coordinate arithmetic of the texture-filtering sampler (sampler 1). The
+ * texture unit's 1/256 weights are discontinuous in the coordinate, so FP64 coordinates would
+ * round an occasional weight the other way than the engine's FP32 ones. The reference itself
+ * forms these coordinates in float (patchMatch.cu:462-505, :543); sampler 1 follows the
+ * engine's explicit single-precision sequence: fused multiply-adds and correctly rounded
+ * reciprocals and products. An exact product of two floats fits a double, so one rounding
+ * of a double sum gives the fused result (double rounding differs only in rare halfway ties).
+ * ---------------------------------------------------------------------------------- */
+static inline float f_fma(float a, float b, float c) { return (float)((double)a * (double)b + (double)c); }
+static inline float f_mul(float a, float b) { return (float)((double)a * (double)b); }
+static inline float f_add(float a, float b) { return (float)((double)a + (double)b); }
+static inline float f_rcp(float a) { return (float)(1.0 / (double)a); }
+
+static float device_scale(const pmo_problem *p, int x)
+{
+    return f_add(f_mul((float)p->orientation[0],
+                       f_fma((float)p->inv_k[0], f_add((float)x, 0.5f), (float)p->inv_k[1])),
+                 (float)p->orientation[2]);
+}
+
+/* T = H1 - s H2 with s = 1/(depth scale), the texture's half-texel offset folded into the
+ * first two rows, evaluated at the window origin (ox, oy): out[0..8] = c0 (3), c1 (3), base (3). */
+static void device_warp(const pmo_problem *p, int view, float depth, float scale, float ox,
+                        float oy, float out[9])
+{
+    const double *hh = p->hh + 18 * (size_t)view;
+    const float s = f_rcp(f_mul(depth, scale));
+    float t[9];
+    for (int i = 0; i < 9; ++i) t[i] = f_fma(-s, (float)hh[9 + i], (float)hh[i]);
+    for (int i = 0; i < 3; ++i) {
+        t[i] = f_fma(0.5f, t[6 + i], t[i]);
+        t[3 + i] = f_fma(0.5f, t[6 + i], t[3 + i]);
+    }
+    out[0] = t[0]; out[1] = t[3]; out[2] = t[6];
+    out[3] = t[1]; out[4] = t[4]; out[5] = t[7];
+    out[6] = f_fma(t[0], ox, f_fma(t[1], oy, t[2]));
+    out[7] = f_fma(t[3], ox, f_fma(t[4], oy, t[5]));
+    out[8] = f_fma(t[6], ox, f_fma(t[7], oy, t[8]));
+}
+
 /* Plane scale s = n^T K^-1 (x + 1/2, y + 1/2, 1): patchMatch.cu:798-800, :876-883 with
  * orientation[1] = 0 (the reference accumulates it row by row; this evaluates it). */
 static inline real plane_scale(const pmo_problem *p, int x)
@@ -324,6 +374,10 @@ static real ncc_eval(const pmo_problem *p, const double *sum_i, const double *su
     for (int i = 0; i < 9; ++i) t[i] = (real)hh[i] - (real)hh[9 + i] / depth / scale;
     const float *src = p->src[view];
     const int sw = p->src_width[view], sh = p->src_height[view];
+    float dw[9];
+    if (p->sampler == 1)
+        device_warp(p, view, (float)depth, device_scale(p, x), (float)(x - hw) + 0.5f,
+                    (float)(y - hw) + 0.5f, dw);
     int lead = 0;
     if (p->quirks) lead = axis == 0 ? (hw - x > 0 ? hw - x : 0) : (hw - y > 0 ? hw - y : 0);
 
@@ -336,11 +390,24 @@ static real ncc_eval(const pmo_problem *p, const double *sum_i, const double *su
         for (int dx = 0; dx < w; ++dx) {
             int xx = x - hw + dx;
             if (xx < 0 || xx >= W) continue;
-            real px = (real)xx + (real)0.5, py = (real)yy + (real)0.5;
-            real u = t[0] * px + t[1] * py + t[2];
-            real v = t[3] * px + t[4] * py + t[5];
-            real z = t[6] * px + t[7] * py + t[8];
-            real jv = sample_bilinear(src, sw, sh, u / z, v / z, p->sampler);
+            real jv;
+            if (p->sampler == 1) {
+                const float fdx = (float)dx, fdy = (float)dy;
+                const float pu = f_fma(dw[0], fdx, f_fma(dw[3], fdy, dw[6]));
+                const float pv = f_fma(dw[1], fdx, f_fma(dw[4], fdy, dw[7]));
+                float pz = f_fma(dw[2], fdx, f_fma(dw[5], fdy, dw[8]));
+                pz = fabsf(pz) < 1e-20f ? 1e-20f : pz;
+                const float r = f_rcp(pz);
+                /* texture coordinates carry the half-texel offset; texel i sits at i + 1/2 */
+                jv = sample_bilinear(src, sw, sh, (real)((double)f_mul(pu, r) - 0.5),
+                                     (real)((double)f_mul(pv, r) - 0.5), 1);
+            } else {
+                real px = (real)xx + (real)0.5, py = (real)yy + (real)0.5;
+                real u = t[0] * px + t[1] * py + t[2];
+                real v = t[3] * px + t[4] * py + t[5];
+                real z = t[6] * px + t[7] * py + t[8];
+                jv = sample_bilinear(src, sw, sh, u / z, v / z, 0);
+            }
             int rx = axis == 0 ? xx - lead : xx;
             int ry = axis == 0 ? yy : yy - lead;
             real iv = texel(p->ref, W, H, rx, ry);
@@ -448,16 +515,15 @@ int pmo_find_min_cost(const double cost[3])
 
 /* ------------------------------------------------------------------------------------
  * Initial depth, generate_kernel_float (array2d_wrapper.cu:3-20):
- * depth = (1 - U(0,1]) * (far - near) + near.
+ * depth = (1 - U(0,1]) * (far - near) + near, in float like the reference's depth map.
  * ---------------------------------------------------------------------------------- */
 void pmo_init_depth(const pmo_problem *p, double *depth)
 {
     const int n = p->width * p->height;
-    const real span = (real)p->depth_far - (real)p->depth_near;
     #pragma omp parallel for schedule(static)
     for (int i = 0; i < n; ++i) {
-        real u = draw(p, i, 0xFFFFFFFFu, PMO_RNG_INIT, 0);
-        depth[i] = (double)(((real)1 - u) * span + (real)p->depth_near);
+        const float u = (float)draw(p, i, 0xFFFFFFFFu, PMO_RNG_INIT, 0);
+        depth[i] = float_depth((double)(1.0f - u), p->depth_near, p->depth_far);
     }
 }
 
@@ -509,7 +575,6 @@ long long pmo_sweep(const pmo_problem *p, const double *sum_i, const double *sum
     const int axis = rotated ? 1 : 0;
     const real a2 = alpha_sq(p->sp_alpha);
     const real u_emit = uniform_emission(a2);
-    const real d_near = (real)p->depth_near, d_span = (real)p->depth_far - (real)p->depth_near;
     if (line_begin < 0) line_begin = 0;
     if (line_end < 0 || line_end > nlines) line_end = nlines;
     long long evals = 0;
@@ -569,7 +634,8 @@ long long pmo_sweep(const pmo_problem *p, const double *sum_i, const double *sum
                 for (int v = 0; v < V; ++v) cdf[v] /= cdf[V - 1];
 
                 const real d_cur = (real)depth[pix];
-                const real d_rand = draw(p, pix, sweep_id, PMO_RNG_RAND_DEPTH, 0) * d_span + d_near;
+                const real d_rand = (real)float_depth((double)draw(p, pix, sweep_id, PMO_RNG_RAND_DEPTH, 0),
+                                                      p->depth_near, p->depth_far);
                 real c3[3] = {0, 0, 0};
                 int tested = 0;
                 for (int j = 0; j < S; ++j) {

@@ -61,7 +61,8 @@ typedef struct pmo_problem {
                                        misalignment at the leading edge (:546)            */
     int sampler;                    /* 0: exact bilinear weights; 1: texture-unit weights
                                        (fractions rounded half-up to 1/256, cross term
-                                       alpha*beta rounded likewise)                       */
+                                       alpha*beta rounded likewise) on single-precision
+                                       coordinates formed as the engine forms them        */
 } pmo_problem;
 
 void pmo_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);

@@ -235,7 +235,9 @@ __device__ __forceinline__ void load_window(const RefDesc &D, int x, int y, int 
     pw.bsum = shifted ? warp_sum(bs) : 0.0f;
     pw.ox = (float)x0 + 0.5f;
     pw.oy = (float)y0 + 0.5f;
-    pw.scale = D.nx * (D.ik00 * ((float)x + 0.5f) + D.ik02) + D.nz;
+    // explicit IEEE operations: the texture-filtering sampler's coordinates are replicated
+    // bit for bit by the oracle
+    pw.scale = __fadd_rn(__fmul_rn(D.nx, fmaf(D.ik00, __fadd_rn((float)x, 0.5f), D.ik02)), D.nz);
 }
 
 // 1 - NCC (patchMatch.cu:594-610): 2 when every source sample is zero, variances below 1e-5
@@ -267,7 +269,8 @@ __device__ __forceinline__ WarpSetup warp_setup(const RefDesc &D, int view, floa
     // 20 floats per view: H1 (row-major, floats 0-8), H2 (floats 9-17), 2 pad.
     const float h1[9] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x};
     const float h2[9] = {c.y, c.z, c.w, d.x, d.y, d.z, d.w, e.x, e.y};
-    const float s = __fdividef(1.0f, depth * scale);
+    // texture-filtering sampler: correctly rounded, so the oracle reproduces the coordinates
+    const float s = HW ? __frcp_rn(__fmul_rn(depth, scale)) : __fdividef(1.0f, depth * scale);
     float t[9];
 #pragma unroll
     for (int i = 0; i < 9; ++i) t[i] = fmaf(-s, h2[i], h1[i]);
@@ -299,8 +302,8 @@ __device__ __forceinline__ float warp_sample(const WarpSetup &A, cudaTextureObje
         // keep the coordinate finite on the source camera's principal plane (border -> 0);
         // px, py already carry the texture's half-texel offset
         pz = fabsf(pz) < 1e-20f ? 1e-20f : pz;
-        const float r = __fdividef(1.0f, pz);
-        return tex2DLayered<float>(tex, px * r, py * r, layer);
+        const float r = __frcp_rn(pz);
+        return tex2DLayered<float>(tex, __fmul_rn(px, r), __fmul_rn(py, r), layer);
     }
     const float r = __fdividef(1.0f, pz);
     return sample_source_nb(tex, px * r, py * r, sw, sh);

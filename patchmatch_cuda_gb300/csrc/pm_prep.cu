@@ -93,7 +93,7 @@ __global__ void init_depth_kernel(const RefDesc *refs, int r, int npix)
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= npix) return;
     const float u = draw_uniform(D.seed, (uint32_t)i, INIT_SWEEP_ID, RNG_INIT, 0, D.batch_id);
-    D.depth[i] = (1.0f - u) * D.depth_span + D.depth_near;
+    D.depth[i] = fmaf(1.0f - u, D.depth_span, D.depth_near);
 }
 
 __global__ void sample_kernel(const RefDesc *refs, int r, int view, int n,

@@ -154,7 +154,7 @@ sweep_kernel(const __grid_constant__ SweepArgs A)
 
         // random depth and view samples, first view with u <= CDF (:937-961)
         const float d_rand =
-            draw_uniform(seed, pix, sweep, RNG_RAND_DEPTH, 0, batch) * D.depth_span + D.depth_near;
+            fmaf(draw_uniform(seed, pix, sweep, RNG_RAND_DEPTH, 0, batch), D.depth_span, D.depth_near);
         const float u_mine = lane < S ? draw_uniform(seed, pix, sweep, RNG_SAMPLE, lane, batch) : 2.0f;
         int my_sel = -1;
         unsigned umask = 0;
