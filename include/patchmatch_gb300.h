@@ -226,6 +226,14 @@ pm_status pm_box_moments_noalloc(const float *d_ref, size_t ref_pitch, int width
  * Device-side Philox4x32-10 for n counters; out gets 4 words per counter. */
 pm_status pm_philox(uint64_t seed, int n, const uint32_t *counters, uint32_t *out);
 
+/* ---- reciprocal check ---------------------------------------------------------------------
+ * No counterpart in the reference (whose fast-math divides are not reproducible on a CPU):
+ * the texture-filtering sampler forms 1/z with a Newton-refined hardware reciprocal so that
+ * its coordinates equal the correctly rounded ones the CPU oracle forms. Counts, over every
+ * significand of the binades [2^e, 2^(e+1)) and their negatives, the values where that
+ * reciprocal differs from the correctly rounded one (expected: 0). */
+pm_status pm_check_reciprocal(int exp_shift, unsigned long long *mismatches);
+
 #ifdef __cplusplus
 }
 #endif

@@ -393,9 +393,10 @@ static real ncc_eval(const pmo_problem *p, const double *sum_i, const double *su
             real jv;
             if (p->sampler == 1) {
                 const float fdx = (float)dx, fdy = (float)dy;
-                const float pu = f_fma(dw[0], fdx, f_fma(dw[3], fdy, dw[6]));
-                const float pv = f_fma(dw[1], fdx, f_fma(dw[4], fdy, dw[7]));
-                float pz = f_fma(dw[2], fdx, f_fma(dw[5], fdy, dw[8]));
+                /* the engine walks down window column dx: column base, then row dy */
+                const float pu = f_fma(dw[3], fdy, f_fma(dw[0], fdx, dw[6]));
+                const float pv = f_fma(dw[4], fdy, f_fma(dw[1], fdx, dw[7]));
+                float pz = f_fma(dw[5], fdy, f_fma(dw[2], fdx, dw[8]));
                 pz = fabsf(pz) < 1e-20f ? 1e-20f : pz;
                 const float r = f_rcp(pz);
                 /* texture coordinates carry the half-texel offset; texel i sits at i + 1/2 */

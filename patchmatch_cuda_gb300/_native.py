@@ -33,7 +33,7 @@ EXPORTED_SYMBOLS = [
     "pm_save_depth", "pm_get_stats", "pm_get_stream", "pm_get_size", "pm_init_depth",
     "pm_compute_costs", "pm_run_sweep", "pm_set_depth", "pm_get_costs", "pm_set_costs",
     "pm_get_ref_maps", "pm_get_source_texels", "pm_eval_costs", "pm_sample_source",
-    "pm_transpose_layers", "pm_philox", "pm_box_moments_noalloc",
+    "pm_transpose_layers", "pm_philox", "pm_box_moments_noalloc", "pm_check_reciprocal",
 ]
 
 
@@ -111,6 +111,7 @@ def load_engine() -> C.CDLL:
         "pm_sample_source": (C.c_int, [H, C.c_int, C.c_int, P, P, P]),
         "pm_transpose_layers": (C.c_int, [P, C.c_size_t, P, C.c_size_t, C.c_int, C.c_int, C.c_int, P]),
         "pm_philox": (C.c_int, [C.c_uint64, C.c_int, P, P]),
+        "pm_check_reciprocal": (C.c_int, [C.c_int, P]),
         "pm_box_moments_noalloc": (C.c_int, [P, C.c_size_t, C.c_int, C.c_int, C.c_int, P, P, P, C.c_size_t, P]),
     }
     for name, (res, args) in sig.items():

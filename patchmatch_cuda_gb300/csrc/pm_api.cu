@@ -1126,4 +1126,20 @@ pm_status pm_philox(uint64_t seed, int n, const uint32_t *counters, uint32_t *ou
     return PM_OK;
 }
 
+pm_status pm_check_reciprocal(int exp_shift, unsigned long long *mismatches)
+{
+    if (!mismatches || exp_shift < -120 || exp_shift > 120) return PM_ERR_INVALID_ARGUMENT;
+    unsigned long long *d = nullptr;
+    if (cudaMalloc((void **)&d, sizeof *d) != cudaSuccess) {
+        cudaGetLastError();
+        return PM_ERR_OUT_OF_MEMORY;
+    }
+    cudaError_t e = cudaMemset(d, 0, sizeof *d);
+    if (e == cudaSuccess) e = launch_check_rcp(exp_shift, d, nullptr);
+    if (e == cudaSuccess) e = cudaMemcpy(mismatches, d, sizeof *d, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) { cudaGetLastError(); return PM_ERR_CUDA; }
+    return PM_OK;
+}
+
 }  // extern "C"

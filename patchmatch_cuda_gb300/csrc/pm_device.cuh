@@ -1,11 +1,13 @@
 // pm_device.cuh -- device building blocks of the PatchMatch engine (sm_103a).
 //
-// One warp owns one line of a sweep (a reference-image column for vertical sweeps, a row
-// for horizontal ones). For a windowed NCC every lane owns ceil(w*w/32) "slots" of the
-// window: slot i of lane l is window sample k = l + 32 i, (dx, dy) = (k % w, k / w). The
-// reference values of a lane's slots are loaded once per step into registers and reused
-// by every hypothesis of that step; the three source moments of an evaluation are summed
-// per lane and then across the warp with a butterfly of shuffles.
+// A windowed NCC maps lanes to window columns and loops over the window's rows, so the
+// projective coordinates of a lane's samples advance along one column of the homography and
+// every lane reads its reference values from a shared table without bank conflicts. Windows
+// up to 16 wide give each half-warp its own hypothesis (two evaluations per warp pass); wider
+// windows give every lane one or two columns of both hypotheses. Moments are accumulated per
+// column shifted by the column's first sample and combined across lanes exactly (a window
+// mean first, then the centred second moment and covariance), which is accurate in FP32
+// without keeping the samples.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -122,6 +124,22 @@ __device__ __forceinline__ float sample_source_nb(cudaTextureObject_t tex, float
     return in ? fmaf(ay, bot - top, top) : 0.0f;
 }
 
+// 1/x rounded to nearest for normal x whose reciprocal is normal, without a slow path: the
+// hardware approximation (rcp.approx) refined by two Newton-Raphson corrections
+// r <- r + r (1 - x r), each residual formed exactly by a fused multiply-add (Markstein's
+// correction step, IBM J. Res. Dev. 34(1), 1990). pm_check_reciprocal compares it with the
+// correctly rounded reciprocal over every significand of a binade; the result depends only
+// on the significand inside that range.
+__device__ __forceinline__ float rcp_nr(float x)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    float e = fmaf(-x, r, 1.0f);
+    r = fmaf(r, e, r);
+    e = fmaf(-x, r, 1.0f);
+    return fmaf(r, e, r);
+}
+
 __device__ __forceinline__ float warp_sum(float v)
 {
 #pragma unroll
@@ -151,44 +169,46 @@ __device__ __forceinline__ float msg_forward(float m, float e, float u)
     return ftz(zn0 / (zn0 + zn1));
 }
 
-// ---- window slots ---------------------------------------------------------------------------
+// ---- windows ---------------------------------------------------------------------------------
+// A window's samples are addressed as (dx, dy), 0 <= dx, dy < W. An evaluation maps lanes to
+// window columns and loops over the rows: for W <= 16 each half-warp runs its own evaluation
+// (lane & 15 = column), for larger windows the warp runs both evaluations of a pair with lane
+// (and lane + 32) as columns.
 template <int W>
 struct Window {
     static constexpr int HW = W / 2;
     static constexpr int NSAMP = W * W;
-    static constexpr int NS = (NSAMP + 31) / 32;
+    static constexpr int TAB = ((NSAMP + 31) / 32) * 32;  // table entries, padded
+    static constexpr bool HALF = W <= 16;
+    static constexpr int COLS = HALF ? 1 : (W + 31) / 32;  // columns per lane
 };
 
-// Per-step state of one pixel's window, held by every lane for its own slots.
-//
-// The reference evaluates 1 - (S_IJ - S_I S_J / n) / sqrt(c1 c2) from raw sums
-// (patchMatch.cu:594-610), which cancels badly in FP32 for weakly textured windows. Here
-//   c1 = S_II - S_I^2 / n          comes from the FP64 preparation pass (per pixel),
-//   c2 = sum (J - mu_J)^2          is summed from source samples centred on their own mean,
-//   cov = sum (J - mu_J)(R - mu) + mu_J * sum (R - mu)
-// with mu = S_I / n the reference window mean and R the reference value the reference pairs
-// with each source sample. In exact arithmetic this equals the reference's covariance,
-// including its leading-edge misalignment (the last term is zero for aligned windows).
-template <int W>
-struct PixelWindow {
-    static constexpr int NS = Window<W>::NS;
-    float *b;            // this warp's shared table: b[32 * i + lane] = R - mu of slot i
-    uint64_t inb;        // slot in bounds
-    bool full;           // the whole window lies inside the reference image
+// Scalars of one pixel's reference window. The values b = R - mu of its samples live in a
+// table tab[dy * W + dx] (zero outside the image) with the column sums col[dx] = sum_dy b;
+// mu = S_I / n is the window mean over its n in-bounds pixels and R the reference value the
+// reference pairs with the source sample: the sample at the same position, except at the
+// leading edge where the reference's pairing is shifted over the out-of-bounds columns
+// (patchMatch.cu:546; kept when quirks are on).
+struct WinCtl {
     float ox, oy;        // window origin in reference pixel-centre coordinates
-    float n, inv_n;      // in-bounds count
-    float c1;            // reference variance term, clamped
-    float bsum;          // sum over in-bounds slots of (R_paired - mu); 0 when aligned
-    float scale;         // plane scale at this pixel
+    float scale;         // plane scale at the pixel
+    float c1;            // S_II - S_I^2 / n (FP64 preparation), clamped
+    float inv_n;         // 1 / n
+    float rows, inv_rows;  // in-bounds rows
+    float bsum;          // sum over in-bounds samples of (R_paired - R): 0 unless shifted
+    int x0, y0;          // window origin in pixels
+    int full;            // the window lies inside the image
+    int dy_lo, dy_hi;    // in-bounds rows
 };
 
-// Loads a pixel's window for lane `lane`. axis selects which image axis is the sweep's
-// column axis for the reference's misalignment (0: x, vertical sweeps; 1: y).
+// Loads pixel (x, y)'s window with one warp, lane c owning columns c and c + 32. axis selects
+// which image axis is the sweep's column axis for the leading-edge shift (0: x, vertical
+// sweeps; 1: y).
 template <int W>
 __device__ __forceinline__ void load_window(const RefDesc &D, int x, int y, int axis, int lane,
-                                            const float2 *slots, float *btab, PixelWindow<W> &pw)
+                                            float *tab, float *col, WinCtl &wc)
 {
-    constexpr int HW = Window<W>::HW, NS = Window<W>::NS, NSAMP = Window<W>::NSAMP;
+    constexpr int HW = Window<W>::HW;
     const int Wd = D.width, Hd = D.height;
     const int x0 = x - HW, y0 = y - HW;
     int lead_x = 0, lead_y = 0;
@@ -196,81 +216,81 @@ __device__ __forceinline__ void load_window(const RefDesc &D, int x, int y, int 
         if (axis == 0) lead_x = x0 < 0 ? -x0 : 0;
         else lead_y = y0 < 0 ? -y0 : 0;
     }
+    const bool shifted = (lead_x | lead_y) != 0;
     const int cx0 = max(x0, 0), cx1 = min(x + HW, Wd - 1);
     const int cy0 = max(y0, 0), cy1 = min(y + HW, Hd - 1);
-    pw.n = (float)((cx1 - cx0 + 1) * (cy1 - cy0 + 1));
-    pw.full = x0 >= 0 && y0 >= 0 && x + HW < Wd && y + HW < Hd;
-    pw.inv_n = 1.0f / pw.n;
+    const float n = (float)((cx1 - cx0 + 1) * (cy1 - cy0 + 1));
     const size_t pix = (size_t)y * Wd + x;
-    const float mu = __ldg(D.sum_i + pix) / pw.n;
-    pw.c1 = __ldg(D.c1 + pix);
-    uint64_t inb = 0;
-    float bs = 0.0f;
-    const bool shifted = (lead_x | lead_y) != 0;
+    const float mu = __ldg(D.sum_i + pix) / n;
+    float sh = 0.0f;
+    constexpr int CHUNK = W < 16 ? W : 16;  // rows loaded before any is stored
 #pragma unroll
-    for (int i = 0; i < NS; ++i) {
-        const int k = lane + 32 * i;
-        const float2 o = slots[32 * i + lane];
-        const int xx = x0 + (int)o.x, yy = y0 + (int)o.y;
-        const bool in = (k < NSAMP) && xx >= 0 && xx < Wd && yy >= 0 && yy < Hd;
-        float r = 0.0f;
-        if (in) {
-            r = __ldg(D.ref + (size_t)yy * Wd + xx);
-            if (shifted) {
-                // the reference pairs this source sample with a reference value shifted
-                // back over the leading out-of-bounds columns (zero outside the image)
+    for (int q = 0; q < (W + 31) / 32; ++q) {
+        const int c = lane + 32 * q;
+        if (c >= W) continue;
+        const int xx = x0 + c;
+        const bool col_in = xx >= 0 && xx < Wd;
+        float cs = 0.0f;
+        for (int dy0 = 0; dy0 < W; dy0 += CHUNK) {
+            float rp[CHUNK], ro[CHUNK];
+#pragma unroll
+            for (int i = 0; i < CHUNK; ++i) {
+                const int yy = y0 + dy0 + i;
+                const bool in = dy0 + i < W && col_in && yy >= 0 && yy < Hd;
                 const int rx = xx - lead_x, ry = yy - lead_y;
-                const float rm = (rx >= 0 && ry >= 0) ? __ldg(D.ref + (size_t)ry * Wd + rx) : 0.0f;
-                bs += rm - r;
-                r = rm;
+                rp[i] = (in && rx >= 0 && ry >= 0) ? __ldg(D.ref + (size_t)ry * Wd + rx) : 0.0f;
+                ro[i] = (in && shifted) ? __ldg(D.ref + (size_t)yy * Wd + xx) : 0.0f;
             }
-            inb |= (uint64_t)1 << i;
-            r -= mu;
+#pragma unroll
+            for (int i = 0; i < CHUNK; ++i) {
+                const int dy = dy0 + i, yy = y0 + dy;
+                if (dy >= W) break;
+                const bool in = col_in && yy >= 0 && yy < Hd;
+                const float b = in ? rp[i] - mu : 0.0f;
+                if (in && shifted) sh += rp[i] - ro[i];
+                tab[dy * W + c] = b;
+                cs += b;
+            }
         }
-        btab[32 * i + lane] = r;
+        col[c] = cs;
     }
-    pw.b = btab;
-    pw.inb = inb;
-    // sum(R_paired - mu) = sum(R_paired) - sum(R): exactly zero for aligned windows
-    pw.bsum = shifted ? warp_sum(bs) : 0.0f;
-    pw.ox = (float)x0 + 0.5f;
-    pw.oy = (float)y0 + 0.5f;
-    // explicit IEEE operations: the texture-filtering sampler's coordinates are replicated
-    // bit for bit by the oracle
-    pw.scale = __fadd_rn(__fmul_rn(D.nx, fmaf(D.ik00, __fadd_rn((float)x, 0.5f), D.ik02)), D.nz);
+    if (shifted) sh = warp_sum(sh);
+    if (lane == 0) {
+        wc.ox = (float)x0 + 0.5f;
+        wc.oy = (float)y0 + 0.5f;
+        // explicit IEEE operations: the texture-filtering sampler's coordinates are
+        // replicated bit for bit by the oracle
+        wc.scale = __fadd_rn(__fmul_rn(D.nx, fmaf(D.ik00, __fadd_rn((float)x, 0.5f), D.ik02)), D.nz);
+        wc.c1 = __ldg(D.c1 + pix);
+        wc.inv_n = 1.0f / n;
+        wc.rows = (float)(cy1 - cy0 + 1);
+        wc.inv_rows = 1.0f / wc.rows;
+        wc.bsum = shifted ? sh : 0.0f;
+        wc.x0 = x0;
+        wc.y0 = y0;
+        wc.full = x0 >= 0 && y0 >= 0 && x + HW < Wd && y + HW < Hd;
+        wc.dy_lo = cy0 - y0;
+        wc.dy_hi = cy1 - y0;
+    }
 }
 
-// 1 - NCC (patchMatch.cu:594-610): 2 when every source sample is zero, variances below 1e-5
-// clamp to 0, 1 when their product is 0.
-__device__ __forceinline__ float ncc_finalize(float sj, float c2, float x, float c1, float mu_j,
-                                              float bsum)
-{
-    if (sj == 0.0f) return 2.0f;
-    c2 = c2 < 0.00001f ? 0.0f : c2;
-    const float cc = c1 * c2;
-    if (cc == 0.0f) return 1.0f;
-    return 1.0f - fmaf(mu_j, bsum, x) * rsqrtf(cc);
-}
-
-// Plane-induced homography of (view, depth) applied at the window origin:
-// T = H1 - H2 / (depth * scale) (patchMatch.cu:462-474); returns T's first two columns and
-// T (ox, oy, 1).
+// Plane-induced homography of (view, depth): T = H1 - H2 / (depth * scale)
+// (patchMatch.cu:462-474); its first two columns and T (ox, oy, 1) at the window origin.
 struct WarpSetup {
     float c0x, c0y, c0z, c1x, c1y, c1z, bx, by, bz;
 };
 
 template <bool HW>
-__device__ __forceinline__ WarpSetup warp_setup(const RefDesc &D, int view, float depth,
+__device__ __forceinline__ WarpSetup warp_setup(const float4 *hh, int view, float depth,
                                                 float scale, float ox, float oy)
 {
-    const float4 *h = D.hh + 5 * view;
-    const float4 a = __ldg(h), b = __ldg(h + 1), c = __ldg(h + 2), d = __ldg(h + 3),
-                 e = __ldg(h + 4);
+    const float4 *h = hh + 5 * view;
+    const float4 a = h[0], b = h[1], c = h[2], d = h[3], e = h[4];
     // 20 floats per view: H1 (row-major, floats 0-8), H2 (floats 9-17), 2 pad.
     const float h1[9] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x};
     const float h2[9] = {c.y, c.z, c.w, d.x, d.y, d.z, d.w, e.x, e.y};
     // texture-filtering sampler: correctly rounded, so the oracle reproduces the coordinates
-    const float s = HW ? __frcp_rn(__fmul_rn(depth, scale)) : __fdividef(1.0f, depth * scale);
+    const float s = HW ? rcp_nr(__fmul_rn(depth, scale)) : __fdividef(1.0f, depth * scale);
     float t[9];
 #pragma unroll
     for (int i = 0; i < 9; ++i) t[i] = fmaf(-s, h2[i], h1[i]);
@@ -291,135 +311,201 @@ __device__ __forceinline__ WarpSetup warp_setup(const RefDesc &D, int view, floa
     return w;
 }
 
+// Source sample at homogeneous coordinates (px, py, pz).
 template <bool HW>
-__device__ __forceinline__ float warp_sample(const WarpSetup &A, cudaTextureObject_t tex, int layer,
-                                             float sw, float sh, float dx, float dy)
+__device__ __forceinline__ float fetch(cudaTextureObject_t tex, int layer, float sw, float sh,
+                                       float px, float py, float pz)
 {
-    const float px = fmaf(A.c0x, dx, fmaf(A.c1x, dy, A.bx));
-    const float py = fmaf(A.c0y, dx, fmaf(A.c1y, dy, A.by));
-    float pz = fmaf(A.c0z, dx, fmaf(A.c1z, dy, A.bz));
     if (HW) {
         // keep the coordinate finite on the source camera's principal plane (border -> 0);
         // px, py already carry the texture's half-texel offset
         pz = fabsf(pz) < 1e-20f ? 1e-20f : pz;
-        const float r = __frcp_rn(pz);
+        const float r = rcp_nr(pz);
         return tex2DLayered<float>(tex, __fmul_rn(px, r), __fmul_rn(py, r), layer);
     }
     const float r = __fdividef(1.0f, pz);
     return sample_source_nb(tex, px * r, py * r, sw, sh);
 }
 
-// Whether lane `lane`'s slot i is a window sample: the window may not fill the last slot.
-template <int W>
-__device__ __forceinline__ bool slot_exists(int i, int lane)
+// Moments of one window column under one hypothesis, shifted by the column's first sample K
+// (accurate in FP32 without holding the samples):
+//   s1 = sum (J - K), s2 = sum (J - K)^2, sx = sum (J - K) b
+// over the column's in-bounds samples, b = R - mu from the window table.
+struct ColMoments {
+    float k, s1, s2, sx;
+};
+
+template <int W, bool HW, bool FULL>
+__device__ __forceinline__ void column_moments(const WarpSetup &A, cudaTextureObject_t tex, int layer,
+                                               float sw, float sh, const float *tab, int c,
+                                               bool col_ok, const WinCtl &wc, ColMoments &m)
 {
-    return i < Window<W>::NS - 1 || lane + 32 * i < Window<W>::NSAMP;
+    const int cc = c < W ? c : W - 1;  // idle lanes read a valid entry and discard it
+    const float fc = (float)c;
+    const float colx = fmaf(A.c0x, fc, A.bx), coly = fmaf(A.c0y, fc, A.by), colz = fmaf(A.c0z, fc, A.bz);
+    m.k = m.s1 = m.s2 = m.sx = 0.0f;
+    // the exact sampler's gathers hold four texels each: fewer rows in flight
+    constexpr int UNROLL = HW ? W : 4;
+#pragma unroll UNROLL
+    for (int dy = 0; dy < W; ++dy) {
+        const float fdy = (float)dy;
+        float j = 0.0f;
+        if (col_ok)
+            j = fetch<HW>(tex, layer, sw, sh, fmaf(A.c1x, fdy, colx), fmaf(A.c1y, fdy, coly),
+                          fmaf(A.c1z, fdy, colz));
+        const float b = tab[dy * W + cc];
+        // the shift: row 0's sample (fetched whatever its row's bounds; any finite value works)
+        if (dy == 0) m.k = j;
+        // lanes off the window's columns fetch nothing: j = K = 0 there
+        const float d = (FULL || (dy >= wc.dy_lo && dy <= wc.dy_hi)) ? j - m.k : 0.0f;
+        m.s1 += d;
+        m.s2 = fmaf(d, d, m.s2);
+        m.sx = fmaf(d, b, m.sx);
+    }
 }
 
-// E windowed NCC evaluations (views v[e] at depths d[e], E = 1 or 2) for one pixel; every
-// lane returns the results. Source samples stay in registers for the centred second pass.
-// FULL: the window lies inside the image, so only the last slot needs a test.
-template <int W, int E, bool HW, bool FULL>
-__device__ __forceinline__ void eval_core(const RefDesc &D, const PixelWindow<W> &pw,
-                                          const float2 *slots, int lane, const int (&v)[E],
-                                          const float (&d)[E], float (&out)[E])
+// Per-lane terms of the second reduction stage from the column moments, the column sum bcol
+// of b and the window mean mj: the column's centred second moment and its covariance with
+// the reference.
+__device__ __forceinline__ void column_terms(const ColMoments &m, bool col_ok, float rows,
+                                             float inv_rows, float mj, float bcol, float &c2,
+                                             float &x)
 {
-    constexpr int NS = Window<W>::NS;
-    constexpr int LAST_LANES = Window<W>::NSAMP - 32 * (NS - 1);  // lanes holding the last slot
-    WarpSetup A[E];
-    cudaTextureObject_t tex[E];
-    float sw[E], sh[E];
+    if (!col_ok) return;
+    const float mean = fmaf(m.s1, inv_rows, m.k);
+    const float dm = mean - mj;
+    c2 += fmaf(rows * dm, dm, fmaf(-m.s1 * inv_rows, m.s1, m.s2));
+    x += fmaf(m.k - mj, bcol, m.sx);
+}
+
+// 1 - NCC (patchMatch.cu:594-610): 2 when every source sample is zero, variances below 1e-5
+// clamp to 0, 1 when their product is 0. The reference forms
+// 1 - (S_IJ - S_I S_J / n) / sqrt(c1 c2) from raw sums, which cancels badly in FP32 for weakly
+// textured windows; here c2 = sum (J - mu_J)^2 and the covariance
+// sum (J - mu_J)(R - mu) + mu_J sum (R_paired - R) are assembled from shifted column moments,
+// equal to the reference's in exact arithmetic (the last term, the leading-edge shift, is
+// zero for aligned windows).
+__device__ __forceinline__ float ncc_finalize(bool all_zero, float c2, float x, float c1, float mu_j,
+                                              float bsum)
+{
+    if (all_zero) return 2.0f;
+    c2 = c2 < 0.00001f ? 0.0f : c2;
+    const float cc = c1 * c2;
+    if (cc == 0.0f) return 1.0f;
+    return 1.0f - fmaf(mu_j, bsum, x) * rsqrtf(cc);
+}
+
+// Two windowed NCC evaluations of one pixel, (view va, depth da) and (vb, db); every lane
+// receives both results. hh: the homography table (D.hh or a shared-memory copy). FULL: the
+// window lies inside the reference image.
+template <int W, bool HW, bool FULL>
+__device__ __forceinline__ void ncc_pair_core(const RefDesc &D, const float4 *hh, const WinCtl &wc,
+                                              const float *tab, const float *col, int lane, int va,
+                                              float da, int vb, float db, float &ra, float &rb)
+{
+    if (Window<W>::HALF) {
+        const int half = lane >> 4, c = lane & 15;
+        const int v = half ? vb : va;
+        const WarpSetup A = warp_setup<HW>(hh, v, half ? db : da, wc.scale, wc.ox, wc.oy);
+        const cudaTextureObject_t tex = HW ? D.tex_layered : D.tex[v];
+        const bool col_ok = c < W && (FULL || (unsigned)(wc.x0 + c) < (unsigned)D.width);
+        ColMoments m;
+        column_moments<W, HW, FULL>(A, tex, v, D.src_w[v], D.src_h[v], tab, c, col_ok, wc, m);
+        // stage 1: sum of J over the half (sum = rows K + s1 per column), all-zero test
+        const float rows = FULL ? (float)W : wc.rows;
+        const float inv_rows = FULL ? 1.0f / (float)W : wc.inv_rows;
+        float sj = col_ok ? fmaf(rows, m.k, m.s1) : 0.0f;
 #pragma unroll
-    for (int e = 0; e < E; ++e) {
-        A[e] = warp_setup<HW>(D, v[e], d[e], pw.scale, pw.ox, pw.oy);
-        tex[e] = HW ? D.tex_layered : D.tex[v[e]];
-        sw[e] = D.src_w[v[e]];
-        sh[e] = D.src_h[v[e]];
-    }
-    float smp[E][NS];
-    float j[E];
+        for (int o = 8; o > 0; o >>= 1) sj += __shfl_xor_sync(FULL_MASK, sj, o);
+        const unsigned nz = __ballot_sync(FULL_MASK, col_ok && (m.k != 0.0f || m.s2 != 0.0f));
+        const bool all_zero = ((nz >> (16 * half)) & 0xFFFFu) == 0;
+        const float mj = sj * wc.inv_n;
+        // stage 2: centred second moment and covariance
+        float c2 = 0.0f, x = 0.0f;
+        column_terms(m, col_ok, rows, inv_rows, mj, col[c < W ? c : W - 1], c2, x);
 #pragma unroll
-    for (int e = 0; e < E; ++e) j[e] = 0.f;
+        for (int o = 8; o > 0; o >>= 1) {
+            c2 += __shfl_xor_sync(FULL_MASK, c2, o);
+            x += __shfl_xor_sync(FULL_MASK, x, o);
+        }
+        const float res = ncc_finalize(all_zero, c2, x, wc.c1, mj, wc.bsum);
+        ra = __shfl_sync(FULL_MASK, res, 0);
+        rb = __shfl_sync(FULL_MASK, res, 16);
+    } else {
+        constexpr int COLS = Window<W>::COLS;
+        const int vv[2] = {va, vb};
+        const float dd[2] = {da, db};
+        const float rows = FULL ? (float)W : wc.rows;
+        const float inv_rows = FULL ? 1.0f / (float)W : wc.inv_rows;
+        float out[2];
 #pragma unroll
-    for (int i = 0; i < NS; ++i) {
-        const float2 o = slots[32 * i + lane];
-        // Interior windows sample every full slot unconditionally (no branch between the
-        // fetches, so they can all be in flight at once); the partially filled last slot and
-        // windows cut by the image border keep a per-slot test.
-        const bool guarded = !FULL || (i == NS - 1 && LAST_LANES < 32);
-        const bool take = FULL ? (i < NS - 1 || lane < LAST_LANES) : ((pw.inb >> i) & 1) != 0;
+        for (int e = 0; e < 2; ++e) {
+            const int v = vv[e];
+            const WarpSetup A = warp_setup<HW>(hh, v, dd[e], wc.scale, wc.ox, wc.oy);
+            const cudaTextureObject_t tex = HW ? D.tex_layered : D.tex[v];
+            ColMoments m[COLS];
+            bool ok[COLS];
 #pragma unroll
-        for (int e = 0; e < E; ++e) {
-            float sv = 0.f;
-            if (guarded) {
-                if (take) sv = warp_sample<HW>(A[e], tex[e], v[e], sw[e], sh[e], o.x, o.y);
-            } else {
-                sv = warp_sample<HW>(A[e], tex[e], v[e], sw[e], sh[e], o.x, o.y);
+            for (int q = 0; q < COLS; ++q) {
+                const int c = lane + 32 * q;
+                ok[q] = c < W && (FULL || (unsigned)(wc.x0 + c) < (unsigned)D.width);
+                column_moments<W, HW, FULL>(A, tex, v, D.src_w[v], D.src_h[v], tab, c, ok[q], wc, m[q]);
             }
-            smp[e][i] = sv;
-            j[e] += sv;
+            float sj = 0.0f;
+            bool nzl = false;
+#pragma unroll
+            for (int q = 0; q < COLS; ++q) {
+                if (ok[q]) sj += fmaf(rows, m[q].k, m[q].s1);
+                nzl = nzl || (ok[q] && (m[q].k != 0.0f || m[q].s2 != 0.0f));
+            }
+            sj = warp_sum(sj);
+            const bool all_zero = __ballot_sync(FULL_MASK, nzl) == 0;
+            const float mj = sj * wc.inv_n;
+            float c2 = 0.0f, x = 0.0f;
+#pragma unroll
+            for (int q = 0; q < COLS; ++q) {
+                const int c = lane + 32 * q;
+                column_terms(m[q], ok[q], rows, inv_rows, mj, col[c < W ? c : W - 1], c2, x);
+            }
+            c2 = warp_sum(c2);
+            x = warp_sum(x);
+            out[e] = ncc_finalize(all_zero, c2, x, wc.c1, mj, wc.bsum);
         }
+        ra = out[0];
+        rb = out[1];
     }
-    float m[E], q[E], x[E];
-#pragma unroll
-    for (int e = 0; e < E; ++e) {
-        j[e] = warp_sum(j[e]);
-        m[e] = j[e] * pw.inv_n;
-        q[e] = 0.f;
-        x[e] = 0.f;
-    }
-#pragma unroll
-    for (int i = 0; i < NS; ++i) {
-        const bool take = FULL ? (i < NS - 1 || lane < LAST_LANES) : ((pw.inb >> i) & 1) != 0;
-        const float bi = pw.b[32 * i + lane];
-#pragma unroll
-        for (int e = 0; e < E; ++e) {
-            const float de = take ? smp[e][i] - m[e] : 0.0f;
-            q[e] = fmaf(de, de, q[e]);
-            x[e] = fmaf(de, bi, x[e]);
-        }
-    }
-#pragma unroll
-    for (int e = 0; e < E; ++e) {
-        q[e] = warp_sum(q[e]);
-        x[e] = warp_sum(x[e]);
-        out[e] = ncc_finalize(j[e], q[e], x[e], pw.c1, m[e], pw.bsum);
-    }
+}
+
+// Windows cut by the image border: out of line, so the hot loop stays small.
+template <int W, bool HW>
+__device__ __noinline__ void ncc_pair_edge(const RefDesc &D, const float4 *hh, const WinCtl &wc,
+                                           const float *tab, const float *col, int lane, int va,
+                                           float da, int vb, float db, float &ra, float &rb)
+{
+    ncc_pair_core<W, HW, false>(D, hh, wc, tab, col, lane, va, da, vb, db, ra, rb);
 }
 
 template <int W, bool HW>
-__device__ __forceinline__ float eval_one(const RefDesc &D, const PixelWindow<W> &pw,
-                                          const float2 *slots, int lane, int v, float d)
+__device__ __forceinline__ void ncc_pair(const RefDesc &D, const float4 *hh, const WinCtl &wc,
+                                         const float *tab, const float *col, int lane, int va,
+                                         float da, int vb, float db, float &ra, float &rb)
 {
-    const int vv[1] = {v};
-    const float dd[1] = {d};
-    float out[1];
-    if (pw.full) eval_core<W, 1, HW, true>(D, pw, slots, lane, vv, dd, out);
-    else eval_core<W, 1, HW, false>(D, pw, slots, lane, vv, dd, out);
-    return out[0];
+    if (wc.full) ncc_pair_core<W, HW, true>(D, hh, wc, tab, col, lane, va, da, vb, db, ra, rb);
+    else ncc_pair_edge<W, HW>(D, hh, wc, tab, col, lane, va, da, vb, db, ra, rb);
 }
 
-template <int W, bool HW>
-__device__ __forceinline__ void eval_pair(const RefDesc &D, const PixelWindow<W> &pw,
-                                          const float2 *slots, int lane, int va, float da,
-                                          int vb, float db, float &out_a, float &out_b)
+// Copies a reference's descriptor and homography table into shared memory (all threads of
+// the block take part; synchronise before use). Fields read on every step then never miss in
+// an L1 that texture traffic keeps busy.
+__device__ __forceinline__ void stage_ref(const RefDesc &src, RefDesc &dst, float4 *hh)
 {
-    const int vv[2] = {va, vb};
-    const float dd[2] = {da, db};
-    float out[2];
-    if (pw.full) eval_core<W, 2, HW, true>(D, pw, slots, lane, vv, dd, out);
-    else eval_core<W, 2, HW, false>(D, pw, slots, lane, vv, dd, out);
-    out_a = out[0];
-    out_b = out[1];
-}
-
-// Window offsets (dx, dy) of every lane's slots: table[32 * i + lane] for slot i, filled
-// cooperatively by a CTA (synchronise before use).
-template <int W>
-__device__ __forceinline__ void fill_slot_table(float2 *table)
-{
-    for (int k = threadIdx.x; k < 32 * Window<W>::NS; k += blockDim.x)
-        table[k] = make_float2((float)(k % W), (float)(k / W));
+    static_assert(sizeof(RefDesc) % 4 == 0, "RefDesc is copied in words");
+    const uint32_t *s = reinterpret_cast<const uint32_t *>(&src);
+    uint32_t *d = reinterpret_cast<uint32_t *>(&dst);
+    for (int i = threadIdx.x; i < (int)(sizeof(RefDesc) / 4); i += blockDim.x) d[i] = s[i];
+    const float4 *h = src.hh;
+    const int n = 5 * src.n_src;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) hh[i] = __ldg(h + i);
 }
 
 }  // namespace pm

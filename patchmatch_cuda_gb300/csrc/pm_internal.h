@@ -69,5 +69,6 @@ cudaError_t launch_transpose(const float *in, size_t in_pitch, float *out, size_
                              int w, int h, int layers, cudaStream_t s);
 cudaError_t launch_philox(uint64_t seed, int n, const uint32_t *ctr, uint32_t *out,
                           cudaStream_t s);
+cudaError_t launch_check_rcp(int exp_shift, unsigned long long *mismatches, cudaStream_t s);
 
 }  // namespace pm

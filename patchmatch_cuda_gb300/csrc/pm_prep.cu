@@ -204,4 +204,27 @@ cudaError_t launch_philox(uint64_t seed, int n, const uint32_t *ctr, uint32_t *o
     return cudaGetLastError();
 }
 
+
+// Counts significands of [1, 2) and (-2, -1] (plus 2^k scalings) where rcp_nr differs from
+// the correctly rounded reciprocal.
+__global__ void check_rcp_kernel(int exp_shift, unsigned long long *mismatches)
+{
+    const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= (1u << 23)) return;
+    unsigned bad = 0;
+#pragma unroll
+    for (int sign = 0; sign < 2; ++sign) {
+        const float x = __uint_as_float(((uint32_t)sign << 31) | ((uint32_t)(127 + exp_shift) << 23) | m);
+        bad += __float_as_uint(rcp_nr(x)) != __float_as_uint(__frcp_rn(x));
+    }
+    bad = __reduce_add_sync(FULL_MASK, bad);
+    if ((threadIdx.x & 31) == 0 && bad) atomicAdd(mismatches, (unsigned long long)bad);
+}
+
+cudaError_t launch_check_rcp(int exp_shift, unsigned long long *mismatches, cudaStream_t s)
+{
+    check_rcp_kernel<<<(1u << 23) / 256, 256, 0, s>>>(exp_shift, mismatches);
+    return cudaGetLastError();
+}
+
 }  // namespace pm

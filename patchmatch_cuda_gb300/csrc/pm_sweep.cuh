@@ -1,13 +1,11 @@
 // pm_sweep.cuh -- the PatchMatch kernels templated on the window side W (odd, 3..45).
 //
 //  sweep_kernel<W>  one directional sweep, topToDown / downToTop (patchMatch.cu:818-1209).
-//                   One CTA per line with 1-4 warps. Every warp keeps its own copy of the
-//                   step's window and of the sequential per-step state (messages, CDF,
-//                   samples, argmin: identical arithmetic, so identical values); the NCC
-//                   evaluations of a step are split across the warps and exchanged through
-//                   shared memory.
+//                   One CTA per line with 1-6 warps: warp 0 holds the line's sequential
+//                   state, every warp evaluates NCCs, the next step's reference window is
+//                   loaded one step ahead (see the kernel's comment).
 //  costs_kernel<W>  every view's cost at the current depth, computeAllCostGivenDepth
-//                   (patchMatch.cu:775-816); one warp per pixel.
+//                   (patchMatch.cu:775-816); one warp per pixel, two views per pass.
 //  eval_kernel<W>   windowed NCC for arbitrary (x, y, view, depth, axis) queries.
 #pragma once
 
@@ -16,7 +14,11 @@
 namespace pm {
 
 constexpr int MAX_BATCH_REFS = 256;
-constexpr int MAX_WARPS_PER_LINE = 4;
+constexpr int MAX_WARPS_PER_LINE = 6;
+// Register caps of the sweep kernel: 72 per thread with the texture-filtering sampler (nine
+// 3-warp lines or five 5-warp lines resident per SM); 96 with the exact sampler, whose
+// gathers hold four texels.
+template <bool HW> struct SweepRegs { static constexpr int value = HW ? 72 : 96; };
 constexpr int COST_BLOCK = 128;
 
 struct SweepArgs {
@@ -47,17 +49,63 @@ __device__ __forceinline__ int nth_bit(unsigned m, int t)
     return __ffs(m) - 1;
 }
 
-template <int W, bool HW>
-__global__ void __launch_bounds__(32 * MAX_WARPS_PER_LINE, 4)
-sweep_kernel(const __grid_constant__ SweepArgs A)
+// Per-step decisions of warp 0, published to the line's other warps (double-buffered by step
+// parity: warp 0 writes step k+1's block while slower warps may still read step k's).
+struct StepCtl {
+    unsigned umask;          // views drawn by at least one sample
+    int tested;              // samples that found a view
+    float c1sum;             // sum of the drawn views' current costs, in draw order
+    float d_former, d_rand, d_cur;
+    int8_t sel[MAX_VIEWS];   // view of each draw, -1 when the CDF found none
+};
+
+// The view-sample and random-depth draws of one step, made one step ahead (double-buffered).
+// The cost-2 replacement draws are made by warp 0 when a cost of 2 occurs.
+struct StepDraws {
+    float sample[MAX_VIEWS];  // view samples (RNG_SAMPLE)
+    float depth;              // random depth (RNG_RAND_DEPTH)
+};
+
+__device__ __forceinline__ void make_draws(const RefDesc &D, uint32_t pix, uint32_t sweep, int S,
+                                           int lane, StepDraws &out)
 {
-    constexpr int NS = Window<W>::NS;
+    const uint64_t seed = D.seed;
+    const uint32_t batch = D.batch_id;
+    // lanes below S draw the view samples; the last lane the random depth (when S < 32)
+    const bool depth_lane = lane == 31 && S < 32;
+    if (lane < S || depth_lane) {
+        const float u = draw_uniform(seed, pix, sweep, depth_lane ? RNG_RAND_DEPTH : RNG_SAMPLE,
+                                     depth_lane ? 0 : lane, batch);
+        if (depth_lane) out.depth = u;
+        else out.sample[lane] = u;
+    }
+    if (S >= 32 && lane == 0) out.depth = draw_uniform(seed, pix, sweep, RNG_RAND_DEPTH, 0, batch);
+}
+
+// One directional sweep. One CTA per line of `blockDim.x / 32` warps. Warp 0 owns the line's
+// sequential state (lane = source view): messages, posterior CDF, view samples, the argmin's
+// current costs and the commit of each step; every warp evaluates NCCs. Per step:
+//   before B1  warp 0 samples views and publishes them; warp 1 loads the next step's
+//              reference window and warp 2 makes the draws two steps ahead (double and
+//              triple buffers; with fewer warps the lower ones take these roles on);
+//   B1 .. B2   each drawn view's NCC at the previous step's depth and at the random depth,
+//              both in one pass over the window, the views spread over the warps;
+//   B2 .. B3   every warp forms the same argmin; unless the current depth won, the other
+//              views' NCCs at the chosen depth, two views per pass;
+//   after B3   warp 0 commits the costs, the depth and the forward message.
+template <int W, bool HW>
+__global__ void __maxnreg__(SweepRegs<HW>::value) sweep_kernel(const __grid_constant__ SweepArgs A)
+{
+    constexpr int TAB = Window<W>::TAB;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    const int wpl = blockDim.x >> 5;
+    const int nw = blockDim.x >> 5;
     const int gline = blockIdx.x;
     const int r = find_ref(A, gline);
-    const RefDesc &D = A.refs[r];
+    __shared__ RefDesc D;
+    __shared__ float4 s_hh[5 * MAX_VIEWS];
+    stage_ref(A.refs[r], D, s_hh);
+    __syncthreads();
     const int line = gline - A.line_start[r];
     const int Wd = D.width, Hd = D.height, V = D.n_src;
     const int S = A.num_samples > 0 ? A.num_samples : D.num_samples;
@@ -66,22 +114,27 @@ sweep_kernel(const __grid_constant__ SweepArgs A)
     const int axis = rot ? 1 : 0;
     const int nsteps = rot ? Wd : Hd;
     const float a2 = D.a2, u_emit = D.u_emit;
-    const uint64_t seed = D.seed;
-    const uint32_t batch = D.batch_id, sweep = A.sweep_id;
+    const uint32_t sweep = A.sweep_id;
     const bool vl = lane < V;
     const unsigned all_views = V >= 32 ? FULL_MASK : ((1u << V) - 1u);
     float *cost = D.cost;
     float *bline = D.beta + (size_t)line * nsteps * V;
+    // before B1 of step k, warp 1 loads step k+1's window and warp 2 makes step k+2's draws
+    // (with fewer warps the lower ones take these roles on)
+    const int w_load = nw > 1 ? 1 : 0;
+    const int w_draw = nw > 2 ? 2 : w_load;
+    const int n_eval = nw;
+    // evaluation tasks go to warps 1, 2, ..., nw-1, then 0
+    const int task0 = (warp + n_eval - 1) % n_eval;
 
-    __shared__ float s_res_f[2][MAX_VIEWS];  // NCC(view, previous step's depth), by step parity
-    __shared__ float s_res_r[2][MAX_VIEWS];  // NCC(view, random depth)
-    __shared__ float s_new[MAX_VIEWS];       // refreshed costs
-
-    __shared__ float2 slots[32 * NS];
-    __shared__ float btabs[MAX_WARPS_PER_LINE][32 * NS];
-    float *btab = btabs[warp];
-    fill_slot_table<W>(slots);
-    __syncthreads();
+    __shared__ float s_tab[2][TAB];
+    __shared__ float s_col[2][W];
+    __shared__ WinCtl s_win[2];
+    __shared__ StepDraws s_draw[3];
+    __shared__ StepCtl s_ctl[2];
+    __shared__ float s_res_f[MAX_VIEWS];  // NCC(view, previous step's depth)
+    __shared__ float s_res_r[MAX_VIEWS];  // NCC(view, random depth)
+    __shared__ float s_new[MAX_VIEWS];    // refreshed costs
 
 #define PM_PIXEL(k, x, y)                                    \
     do {                                                     \
@@ -90,8 +143,24 @@ sweep_kernel(const __grid_constant__ SweepArgs A)
         y = rot ? line : c_;                                 \
     } while (0)
 
-    // 1. backward messages in reverse processing order (patchMatch.cu:856-869, :1050-1059)
+    // step k+1's window and step k+2's draws
+    auto prep_step = [&](int k) {
+        int xn, yn;
+        if (warp == w_load && k + 1 < nsteps) {
+            PM_PIXEL(k + 1, xn, yn);
+            load_window<W>(D, xn, yn, axis, lane, s_tab[(k + 1) & 1], s_col[(k + 1) & 1], s_win[(k + 1) & 1]);
+        }
+        if (warp == w_draw && k + 2 < nsteps) {
+            PM_PIXEL(k + 2, xn, yn);
+            make_draws(D, (uint32_t)(yn * Wd + xn), sweep, S, lane, s_draw[(k + 2) % 3]);
+        }
+    };
+
+    float alpha = 0.5f, d_former = 0.0f;
+    float c_next = 0.0f, b_next = 0.0f, d_next = 0.0f;
+    unsigned long long n_alg = 0, n_done = 0;
     if (warp == 0) {
+        // backward messages in reverse processing order (patchMatch.cu:856-869, :1050-1059)
         float beta = 0.5f;
 #pragma unroll 4
         for (int k = nsteps - 1; k >= 0; --k) {
@@ -101,137 +170,200 @@ sweep_kernel(const __grid_constant__ SweepArgs A)
             if (vl) {
                 bline[(size_t)k * V + lane] = beta;
                 float c = cost[(size_t)pix * V + lane];
-                if (c == 2.0f) c = 2.0f * draw_uniform(seed, pix, sweep, RNG_BWD, lane, batch);
+                if (c == 2.0f) c = 2.0f * draw_uniform(D.seed, pix, sweep, RNG_BWD, lane, D.batch_id);
                 beta = msg_backward(beta, emission(c, a2), u_emit);
             }
         }
-    }
-    __syncthreads();
-
-    // 2. forward message at the first step (patchMatch.cu:872-874)
-    float alpha = 0.5f, d_former;
-    {
+        // forward message at the first step (patchMatch.cu:872-874)
         int x, y;
         PM_PIXEL(0, x, y);
         const uint32_t pix = (uint32_t)(y * Wd + x);
         if (vl) {
             float c = cost[(size_t)pix * V + lane];
-            if (c == 2.0f) c = 2.0f * draw_uniform(seed, pix, sweep, RNG_FWD_POST, lane, batch);
+            if (c == 2.0f) c = 2.0f * draw_uniform(D.seed, pix, sweep, RNG_FWD_POST, lane, D.batch_id);
             alpha = msg_forward(0.5f, emission(c, a2), u_emit);
         }
         d_former = D.depth[pix];
+        if (nsteps > 1) {
+            PM_PIXEL(1, x, y);
+            const uint32_t p1 = (uint32_t)(y * Wd + x);
+            if (vl) {
+                c_next = cost[(size_t)p1 * V + lane];
+                b_next = bline[(size_t)V + lane];
+            }
+            d_next = D.depth[p1];
+        }
     }
+    // step k's window in s_tab[k & 1], its draws in s_draw[k % 3]
+    if (warp == w_load && nsteps > 1) {
+        int x, y;
+        PM_PIXEL(1, x, y);
+        load_window<W>(D, x, y, axis, lane, s_tab[1], s_col[1], s_win[1]);
+    }
+    if (warp == w_draw) {
+        for (int k = 1; k < nsteps && k <= 2; ++k) {
+            int x, y;
+            PM_PIXEL(k, x, y);
+            make_draws(D, (uint32_t)(y * Wd + x), sweep, S, lane, s_draw[k]);
+        }
+    }
+    __syncthreads();
 
-    unsigned long long n_alg = 0, n_done = 0;
-    // 3. propagation (patchMatch.cu:888-1000)
+    // propagation (patchMatch.cu:888-1000)
     for (int k = 1; k < nsteps; ++k) {
-        const int par = k & 1;
+        const int buf = k & 1;
         int x, y;
         PM_PIXEL(k, x, y);
         const uint32_t pix = (uint32_t)(y * Wd + x);
-        const float c_old = vl ? cost[(size_t)pix * V + lane] : 0.0f;
-        const float b = vl ? bline[(size_t)k * V + lane] : 0.0f;
-        const float d_cur = D.depth[pix];
-        PixelWindow<W> pw;
-        load_window<W>(D, x, y, axis, lane, slots, btab, pw);
-
-        // forward message with the old costs, posterior, CDF (:905-923)
-        float q = 0.0f;
-        if (vl) {
-            float c = c_old;
-            if (c == 2.0f) c = 2.0f * draw_uniform(seed, pix, sweep, RNG_FWD_PRE, lane, batch);
-            const float a = msg_forward(alpha, emission(c, a2), u_emit);
-            const float z0 = a * b, z1 = (1.0f - a) * (1.0f - b);
-            q = ftz(z0 / (z0 + z1));
-        }
-        float cdf = q;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const float t = __shfl_up_sync(FULL_MASK, cdf, o);
-            if (lane >= o) cdf += t;
-        }
-        cdf = cdf / __shfl_sync(FULL_MASK, cdf, V - 1);
-
-        // random depth and view samples, first view with u <= CDF (:937-961)
-        const float d_rand =
-            fmaf(draw_uniform(seed, pix, sweep, RNG_RAND_DEPTH, 0, batch), D.depth_span, D.depth_near);
-        const float u_mine = lane < S ? draw_uniform(seed, pix, sweep, RNG_SAMPLE, lane, batch) : 2.0f;
+        prep_step(k);
+        float c_old = 0.0f;
         int my_sel = -1;
-        unsigned umask = 0;
-        for (int j = 0; j < S; ++j) {
-            const float uj = __shfl_sync(FULL_MASK, u_mine, j);
-            const unsigned bal = __ballot_sync(FULL_MASK, vl && uj <= cdf);
-            const int view = bal ? __ffs(bal) - 1 : -1;
-            if (lane == j) my_sel = view;
-            if (view >= 0) umask |= 1u << view;
-        }
-
-        // Two phases of NCC evaluations, split across the line's warps (one call site):
-        //  phase 0: every sampled view at the previous step's depth and the random depth;
-        //  phase 1: every view at the chosen depth unless the current depth won (:983-994),
-        //           sampled views reusing phase 0's identical evaluation.
-        const int nu = __popc(umask);
-        int idx = 1, tested = 0, nn = 0;
-        unsigned need = 0;
-        float best = d_cur;
-        for (int phase = 0; phase < 2; ++phase) {
-            const int ntasks = phase == 0 ? 2 * nu : nn;
-            for (int t = warp; t < ntasks; t += wpl) {
-                int v;
-                float d;
-                float *dst;
-                if (phase == 0) {
-                    v = nth_bit(umask, t >> 1);
-                    d = (t & 1) ? d_rand : d_former;
-                    dst = (t & 1) ? &s_res_r[par][v] : &s_res_f[par][v];
-                } else {
-                    v = nth_bit(need, t);
-                    d = best;
-                    dst = &s_new[v];
+        if (warp == 0) {
+            const StepDraws &dr = s_draw[k % 3];
+            c_old = c_next;
+            const float b = b_next;
+            const float d_cur = d_next;
+            if (k + 1 < nsteps) {  // prefetch the next step's costs, message and depth
+                int xn, yn;
+                PM_PIXEL(k + 1, xn, yn);
+                const uint32_t pn = (uint32_t)(yn * Wd + xn);
+                if (vl) {
+                    c_next = cost[(size_t)pn * V + lane];
+                    b_next = bline[(size_t)(k + 1) * V + lane];
                 }
-                const float res = eval_one<W, HW>(D, pw, slots, lane, v, d);
-                if (lane == 0) *dst = res;
+                d_next = D.depth[pn];
             }
-            if (phase == 1 && ntasks == 0) break;
-            __syncthreads();
+            // forward message with the old costs, posterior, CDF (:905-923)
+            float q = 0.0f;
+            if (vl) {
+                float c = c_old;
+                if (c == 2.0f) c = 2.0f * draw_uniform(D.seed, pix, sweep, RNG_FWD_PRE, lane, D.batch_id);
+                const float a = msg_forward(alpha, emission(c, a2), u_emit);
+                const float z0 = a * b, z1 = (1.0f - a) * (1.0f - b);
+                q = ftz(z0 / (z0 + z1));
+            }
+            float cdf = q;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const float t = __shfl_up_sync(FULL_MASK, cdf, o);
+                if (lane >= o) cdf += t;
+            }
+            cdf = cdf / __shfl_sync(FULL_MASK, cdf, V - 1);
+            // random depth and view samples, first view with u <= CDF (:937-961)
+            const float d_rand = fmaf(dr.depth, D.depth_span, D.depth_near);
+            const float u_mine = lane < S ? dr.sample[lane] : 2.0f;
+            StepCtl &C = s_ctl[buf];
+            unsigned umask = 0;
+            int tested = 0;
+            float c1 = 0.0f;
+            for (int j = 0; j < S; ++j) {
+                const float uj = __shfl_sync(FULL_MASK, u_mine, j);
+                const unsigned bal = __ballot_sync(FULL_MASK, vl && uj <= cdf);
+                const int view = bal ? __ffs(bal) - 1 : -1;
+                if (lane == j) my_sel = view;
+                if (view >= 0) {
+                    umask |= 1u << view;
+                    ++tested;
+                    c1 += __shfl_sync(FULL_MASK, c_old, view);
+                }
+            }
+            if (lane < S) C.sel[lane] = (int8_t)my_sel;
+            if (lane == 0) {
+                C.umask = umask;
+                C.tested = tested;
+                C.c1sum = c1;
+                C.d_former = d_former;
+                C.d_rand = d_rand;
+                C.d_cur = d_cur;
+            }
+        }
+        __syncthreads();  // B1
+
+        const StepCtl &C = s_ctl[buf];
+        const WinCtl &wc = s_win[buf];
+        const float *tab = s_tab[buf];
+        const float *col = s_col[buf];
+        const unsigned umask = C.umask;
+        const int nu = __popc(umask);
+        const int tested = C.tested;
+        // phase 0: each drawn view at the previous step's depth and at the random depth, in
+        // one pass; phase 1 (unless the current depth won): every other view's cost at the
+        // chosen depth (:983-994), two views per pass. One call site for both phases.
+        int idx = 1, nn = 0;
+        unsigned need = 0;
+        float best = C.d_cur;
+        for (int phase = 0; phase < 2; ++phase) {
+            const int ntask = phase == 0 ? nu : (nn + 1) >> 1;
+            for (int t = task0; t < ntask; t += n_eval) {
+                int va, vb;
+                float da, db;
+                if (phase == 0) {
+                    va = vb = nth_bit(umask, t);
+                    da = C.d_former;
+                    db = C.d_rand;
+                } else {
+                    va = nth_bit(need, 2 * t);
+                    vb = 2 * t + 1 < nn ? nth_bit(need, 2 * t + 1) : va;
+                    da = db = best;
+                }
+                float ra, rb;
+                ncc_pair<W, HW>(D, s_hh, wc, tab, col, lane, va, da, vb, db, ra, rb);
+                if (lane == 0) {
+                    if (phase == 0) {
+                        s_res_f[va] = ra;
+                        s_res_r[va] = rb;
+                    } else {
+                        s_new[va] = ra;
+                        s_new[vb] = rb;
+                    }
+                }
+            }
+            __syncthreads();  // B2 after phase 0, B3 after phase 1
             if (phase == 1) break;
             // average over the samples in draw order, argmin with ties to the later index
-            // (:965-979)
-            float c0 = 0.0f, c1 = 0.0f, c2 = 0.0f;
-            for (int j = 0; j < S; ++j) {
-                const int view = __shfl_sync(FULL_MASK, my_sel, j);
-                if (view < 0) continue;
-                ++tested;
-                c0 += s_res_f[par][view];
-                c1 += __shfl_sync(FULL_MASK, c_old, view);
-                c2 += s_res_r[par][view];
-            }
+            // (:965-979); every warp forms the same result from the same values
             if (tested > 0) {
+                int sv = -1;
+                float rf = 0.0f, rr = 0.0f;
+                if (lane < S) {
+                    sv = C.sel[lane];
+                    if (sv >= 0) {
+                        rf = s_res_f[sv];
+                        rr = s_res_r[sv];
+                    }
+                }
+                float c0 = 0.0f, c2 = 0.0f;
+                for (int j = 0; j < S; ++j) {
+                    const int view = __shfl_sync(FULL_MASK, sv, j);
+                    const float f = __shfl_sync(FULL_MASK, rf, j), g = __shfl_sync(FULL_MASK, rr, j);
+                    if (view < 0) continue;
+                    c0 += f;
+                    c2 += g;
+                }
                 const float inv = 1.0f / (float)tested;
+                float c1 = C.c1sum;
                 c0 *= inv; c1 *= inv; c2 *= inv;
                 idx = c0 < c1 ? 0 : 1;
                 idx = (idx == 0 ? c0 : c1) < c2 ? idx : 2;
             }
-            best = idx == 0 ? d_former : (idx == 1 ? d_cur : d_rand);
+            best = idx == 0 ? C.d_former : (idx == 1 ? C.d_cur : C.d_rand);
             if (idx == 1) break;
             need = all_views & ~umask;
             nn = __popc(need);
         }
-        d_former = best;
 
-        float c_new = c_old;
-        if (idx != 1) {
-            if (vl) c_new = (umask >> lane) & 1u ? (idx == 0 ? s_res_f[par][lane] : s_res_r[par][lane])
-                                                 : s_new[lane];
-            if (warp == 0) {
-                if (vl) cost[(size_t)pix * V + lane] = c_new;
+        if (warp == 0) {
+            float c_new = c_old;
+            if (idx != 1) {
+                if (vl) {
+                    c_new = (umask >> lane) & 1u ? (idx == 0 ? s_res_f[lane] : s_res_r[lane]) : s_new[lane];
+                    cost[(size_t)pix * V + lane] = c_new;
+                }
                 if (lane == 0) {
                     n_alg += V;
                     n_done += nn;
                 }
             }
-        }
-        if (warp == 0) {
             if (lane == 0) {
                 D.depth[pix] = best;
                 n_alg += 2 * tested;
@@ -239,13 +371,13 @@ sweep_kernel(const __grid_constant__ SweepArgs A)
             }
             if (A.record_views && lane < S)
                 D.view_sel[(size_t)lane * Wd * Hd + pix] = (uint8_t)(my_sel < 0 ? 255 : my_sel);
-        }
-
-        // forward message from the previous step's with the new costs (:996-999)
-        if (vl) {
-            float c = c_new;
-            if (c == 2.0f) c = 2.0f * draw_uniform(seed, pix, sweep, RNG_FWD_POST, lane, batch);
-            alpha = msg_forward(alpha, emission(c, a2), u_emit);
+            // forward message from the previous step's with the new costs (:996-999)
+            if (vl) {
+                float c = c_new;
+                if (c == 2.0f) c = 2.0f * draw_uniform(D.seed, pix, sweep, RNG_FWD_POST, lane, D.batch_id);
+                alpha = msg_forward(alpha, emission(c, a2), u_emit);
+            }
+            d_former = best;
         }
     }
 #undef PM_PIXEL
@@ -255,36 +387,39 @@ sweep_kernel(const __grid_constant__ SweepArgs A)
     }
 }
 
-// All views' costs at the current depth for every pixel of one reference.
+// All views' costs at the current depth for every pixel of one reference; one warp per pixel,
+// two views per pass.
 template <int W, bool HW>
 __global__ void __launch_bounds__(COST_BLOCK) costs_kernel(const RefDesc *refs, int r, int axis)
 {
-    constexpr int NS = Window<W>::NS;
-    const RefDesc &D = refs[r];
+    constexpr int TAB = Window<W>::TAB;
+    __shared__ RefDesc D;
+    __shared__ float4 s_hh[5 * MAX_VIEWS];
+    stage_ref(refs[r], D, s_hh);
+    __syncthreads();
     const int lane = threadIdx.x & 31;
     const int V = D.n_src;
     const int npix = D.width * D.height;
-    __shared__ float2 slots[32 * NS];
-    __shared__ float btabs[COST_BLOCK / 32][32 * NS];
-    float *btab = btabs[threadIdx.x >> 5];
-    fill_slot_table<W>(slots);
-    __syncthreads();
+    __shared__ float tabs[COST_BLOCK / 32][TAB];
+    __shared__ float cols[COST_BLOCK / 32][W];
+    __shared__ WinCtl wcs[COST_BLOCK / 32];
+    float *tab = tabs[threadIdx.x >> 5];
+    float *col = cols[threadIdx.x >> 5];
+    WinCtl &wc = wcs[threadIdx.x >> 5];
     const int warps = (int)((gridDim.x * blockDim.x) >> 5);
     for (int p = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); p < npix; p += warps) {
         const int x = p % D.width, y = p / D.width;
-        PixelWindow<W> pw;
-        load_window<W>(D, x, y, axis, lane, slots, btab, pw);
+        __syncwarp();
+        load_window<W>(D, x, y, axis, lane, tab, col, wc);
+        __syncwarp();
         const float d = D.depth[p];
         float mine = 0.0f;
-        for (int v = 0; v + 1 < V; v += 2) {
+        for (int v = 0; v < V; v += 2) {
+            const int vb = v + 1 < V ? v + 1 : v;
             float na, nb;
-            eval_pair<W, HW>(D, pw, slots, lane, v, d, v + 1, d, na, nb);
+            ncc_pair<W, HW>(D, s_hh, wc, tab, col, lane, v, d, vb, d, na, nb);
             if (lane == v) mine = na;
-            if (lane == v + 1) mine = nb;
-        }
-        if (V & 1) {
-            const float na = eval_one<W, HW>(D, pw, slots, lane, V - 1, d);
-            if (lane == V - 1) mine = na;
+            if (lane == vb) mine = nb;
         }
         if (lane < V) D.cost[(size_t)p * V + lane] = mine;
     }
@@ -300,20 +435,26 @@ __global__ void __launch_bounds__(COST_BLOCK) eval_kernel(const RefDesc *refs, i
                                                           const int4 *q, const float *depths,
                                                           float *out)
 {
-    constexpr int NS = Window<W>::NS;
-    const RefDesc &D = refs[r];
-    const int lane = threadIdx.x & 31;
-    __shared__ float2 slots[32 * NS];
-    __shared__ float btabs[COST_BLOCK / 32][32 * NS];
-    float *btab = btabs[threadIdx.x >> 5];
-    fill_slot_table<W>(slots);
+    constexpr int TAB = Window<W>::TAB;
+    __shared__ RefDesc D;
+    __shared__ float4 s_hh[5 * MAX_VIEWS];
+    stage_ref(refs[r], D, s_hh);
     __syncthreads();
+    const int lane = threadIdx.x & 31;
+    __shared__ float tabs[COST_BLOCK / 32][TAB];
+    __shared__ float cols[COST_BLOCK / 32][W];
+    __shared__ WinCtl wcs[COST_BLOCK / 32];
+    float *tab = tabs[threadIdx.x >> 5];
+    float *col = cols[threadIdx.x >> 5];
+    WinCtl &wc = wcs[threadIdx.x >> 5];
     const int warps = (int)((gridDim.x * blockDim.x) >> 5);
     for (int i = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); i < n; i += warps) {
         const int4 t = q[i];  // x, y, view, axis
-        PixelWindow<W> pw;
-        load_window<W>(D, t.x, t.y, t.w, lane, slots, btab, pw);
-        const float v = eval_one<W, HW>(D, pw, slots, lane, t.z, depths[i]);
+        __syncwarp();
+        load_window<W>(D, t.x, t.y, t.w, lane, tab, col, wc);
+        __syncwarp();
+        float v, unused;
+        ncc_pair<W, HW>(D, s_hh, wc, tab, col, lane, t.z, depths[i], t.z, depths[i], v, unused);
         if (lane == 0) out[i] = v;
     }
 }
