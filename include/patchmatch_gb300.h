@@ -78,7 +78,10 @@ typedef enum pm_texel_format {
 } pm_texel_format;
 
 typedef enum pm_init_mode {
-    PM_INIT_RANDOM = 0          /* uniform depth in [near, far) (array2d_wrapper.cu:3-20)      */
+    PM_INIT_RANDOM = 0,         /* uniform depth in [near, far) (array2d_wrapper.cu:3-20)      */
+    PM_INIT_PROPOSAL = 1        /* the learned proposal (pm_set_proposal); pixels whose
+                                   confidence is below proposal_threshold keep the uniform
+                                   random depth. No counterpart in the reference.           */
 } pm_init_mode;
 
 typedef enum pm_direction {     /* sweep order within one iteration (patchMatch.cu:344-391) */
@@ -119,6 +122,15 @@ typedef struct pm_params {
     int block_dim_x, block_dim_y;  /* accepted for signature parity, unused                  */
     int sampler;                   /* pm_sampler                                             */
     int texel_format;              /* pm_texel_format                                        */
+    int num_sweeps;                /* 0: all num_iterations x 4 sweeps; else the schedule
+                                      stops after this many sweeps                          */
+    float proposal_threshold;      /* PM_INIT_PROPOSAL: minimum confidence (default 0.5)     */
+    float perturbation;            /* 0 (default): the random hypothesis is uniform in
+                                      [near, far] (patchMatch.cu:937). > 0: no counterpart in
+                                      the reference; half of the pixels (by a second Philox
+                                      word) instead draw within +-perturbation x 2^(-k/4)
+                                      (relative) of their current depth in sweep k, a local
+                                      search that refines a learned initialisation         */
 } pm_params;
 
 typedef struct pm_handle pm_handle;
@@ -233,6 +245,69 @@ pm_status pm_philox(uint64_t seed, int n, const uint32_t *counters, uint32_t *ou
  * significand of the binades [2^e, 2^(e+1)) and their negatives, the values where that
  * reciprocal differs from the correctly rounded one (expected: 0). */
 pm_status pm_check_reciprocal(int exp_shift, unsigned long long *mismatches);
+
+/* ---- learned proposal on a handle -------------------------------------------------------
+ * No counterpart in the reference. pm_set_proposal attaches a network (not owned; NULL
+ * detaches) whose batch is 1 and whose size is the handle's proposal size (pm_proposal_input
+ * with d_out NULL reports it): ceil16(width / 4) x ceil16(height / 4). With init_mode
+ * PM_INIT_PROPOSAL, pm_run then builds the network input from the reference and the two
+ * source views nearest to it, runs the network on the handle's stream and initialises the
+ * depth map from its output. A network attached to several handles must not be run by them
+ * concurrently. pm_proposal_input writes the network input (DEVICE FP32 [height][width][17])
+ * for training; d_out may be NULL. */
+typedef struct pm_net pm_net;
+pm_status pm_set_proposal(pm_handle *h, pm_net *net);
+pm_status pm_proposal_input(pm_handle *h, float *d_out, int *height, int *width);
+
+/* ---- learned depth proposal: tensor-core GEMM -----------------------------------------
+ * No counterpart in the reference (its initial depth is uniformly random,
+ * array2d_wrapper.cu:3-20); the building block of the proposal network's convolutions.
+ * C[m, n] (+)= A[m, k] . B[n, k]^T on DEVICE memory, A and B BF16 with k contiguous (leading
+ * dimensions lda, ldb in elements), on the fifth-generation tensor cores with an FP32
+ * accumulator. mode 0: C is BF16, C = act(A B^T + bias); mode 1: C is FP32, C = A B^T + bias;
+ * mode 2: C is FP32, C += A B^T, with k split over `splits` CTAs. act is ReLU when relu != 0.
+ * m % 128 == 0, n % 16 == 0, k % 64 == 0, leading dimensions multiples of 8, pointers
+ * 16-byte aligned; otherwise PM_ERR_INVALID_ARGUMENT. d_bias (n floats) may be NULL. The work
+ * is enqueued on `stream` (NULL: the default stream). A pipeline wait that times out sets an
+ * error word, read (and optionally cleared) with pm_gemm_error. */
+pm_status pm_gemm_bf16(const void *d_a, int lda, const void *d_b, int ldb, int m, int n, int k,
+                       void *d_c, int ldc, int mode, const float *d_bias, int relu, int splits,
+                       void *stream);
+pm_status pm_gemm_error(unsigned *out, int clear);
+
+/* ---- learned depth proposal: the network --------------------------------------------------
+ * No counterpart in the reference. A 5-level BF16 encoder-decoder (widths 32, 64, 96, 128,
+ * 128; 3x3 convolutions with ReLU, nearest upsampling with skip concatenation, 1x1 head) on
+ * inputs of 17 channels at a quarter of the reference resolution: the reference image and two
+ * source images warped onto 8 fronto-parallel depths. Output per pixel: the normalised inverse
+ * depth s in [0, 1] (depth = 1 / (1/far + s (1/near - 1/far))) and a confidence in [0, 1].
+ * Every convolution runs on pm_gemm_bf16's kernel; training uses the same kernels backward.
+ * A pm_net is sized for one batch and level-0 size (height, width multiples of 16); weights
+ * move between nets of different sizes with pm_net_get_params / pm_net_set_params (FP32,
+ * per layer: weights [cout][ky][kx][cin] then bias [cout]). seed fixes the initial weights. */
+pm_status pm_net_create(int batch, int height, int width, uint64_t seed, pm_net **out);
+pm_status pm_net_destroy(pm_net *net);
+pm_status pm_net_num_params(const pm_net *net, size_t *n);
+pm_status pm_net_size(const pm_net *net, int *batch, int *height, int *width);
+pm_status pm_net_get_params(pm_net *net, float *dst, size_t n);
+pm_status pm_net_set_params(pm_net *net, const float *src, size_t n);
+/* d_input: DEVICE FP32 [batch][height][width][17]; d_out (may be NULL): DEVICE FP32
+ * [batch][height][width][2] = (s, confidence). */
+pm_status pm_net_forward(pm_net *net, const float *d_input, float *d_out, void *stream);
+/* Loss and gradients for d_target (DEVICE FP32 [batch][height][width], normalised inverse
+ * depth; < 0 masks a pixel): L1 of the relative inverse-depth error |inv - inv_t| / inv_t
+ * (inv = inv_far + s inv_range) plus 0.1 x binary cross-entropy of the confidence against
+ * "depth within 2 % of the target's". grad_out (HOST, n_grad floats, may be NULL) receives
+ * dLoss/dparam with the loss taken as sum over pixels / (batch height width); loss_out (may be
+ * NULL) gets 3 floats: mean relative error, mean BCE, valid pixel count. */
+pm_status pm_net_gradients(pm_net *net, const float *d_input, const float *d_target, float inv_far,
+                           float inv_range, float *grad_out, size_t n_grad, float *loss_out);
+/* One Adam step (learning rate lr, betas 0.9 / 0.999) on that loss. */
+pm_status pm_net_train_step(pm_net *net, const float *d_input, const float *d_target, float inv_far,
+                            float inv_range, float lr, float *loss_out);
+/* Layer table: 8 ints per layer (cin, cout, ksize, stride, relu, param offset, input height,
+ * input width). */
+pm_status pm_net_layout(const pm_net *net, int *n_layers, int *desc, int max_layers);
 
 #ifdef __cplusplus
 }

@@ -576,6 +576,7 @@ long long pmo_sweep(const pmo_problem *p, const double *sum_i, const double *sum
     const int axis = rotated ? 1 : 0;
     const real a2 = alpha_sq(p->sp_alpha);
     const real u_emit = uniform_emission(a2);
+    const float perturb = p->perturbation > 0.0f ? p->perturbation * exp2f(-0.25f * (float)sweep_id) : 0.0f;
     if (line_begin < 0) line_begin = 0;
     if (line_end < 0 || line_end > nlines) line_end = nlines;
     long long evals = 0;
@@ -635,8 +636,24 @@ long long pmo_sweep(const pmo_problem *p, const double *sum_i, const double *sum
                 for (int v = 0; v < V; ++v) cdf[v] /= cdf[V - 1];
 
                 const real d_cur = (real)depth[pix];
-                const real d_rand = (real)float_depth((double)draw(p, pix, sweep_id, PMO_RNG_RAND_DEPTH, 0),
-                                                      p->depth_near, p->depth_far);
+                real d_rand;
+                {
+                    const uint32_t ctr[4] = {(uint32_t)pix, sweep_id, ((uint32_t)PMO_RNG_RAND_DEPTH << 16), p->batch_id};
+                    const uint32_t key[2] = {(uint32_t)p->seed, (uint32_t)(p->seed >> 32)};
+                    uint32_t o[4];
+                    pmo_philox4x32_10(ctr, key, o);
+                    const float u = (float)((o[0] >> 8) + 1u) * (1.0f / 16777216.0f);
+                    const float u2 = (float)((o[1] >> 8) + 1u) * (1.0f / 16777216.0f);
+                    d_rand = (real)float_depth((double)u, p->depth_near, p->depth_far);
+                    if (perturb > 0.0f && u2 >= 0.5f) {
+                        /* the engine's local search, in its single-precision arithmetic */
+                        const float lo = (float)p->depth_near;
+                        const float hi = f_add(lo, (float)((double)(float)p->depth_far - (double)lo));
+                        float dr = f_mul((float)d_cur, f_fma(perturb, f_fma(2.0f, u, -1.0f), 1.0f));
+                        dr = dr < lo ? lo : (dr > hi ? hi : dr);
+                        d_rand = (real)dr;
+                    }
+                }
                 real c3[3] = {0, 0, 0};
                 int tested = 0;
                 for (int j = 0; j < S; ++j) {

@@ -63,6 +63,10 @@ typedef struct pmo_problem {
                                        (fractions rounded half-up to 1/256, cross term
                                        alpha*beta rounded likewise) on single-precision
                                        coordinates formed as the engine forms them        */
+    float perturbation;             /* 0: uniform random hypothesis (the reference). > 0: the
+                                       engine's local search: half of the pixels (second
+                                       Philox word >= 1/2) draw within +-perturbation x
+                                       2^(-sweep/4) of their current depth                */
 } pmo_problem;
 
 void pmo_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);

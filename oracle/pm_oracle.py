@@ -33,7 +33,7 @@ class _Problem(C.Structure):
         ("hh", C.c_void_p), ("inv_k", C.c_double * 4), ("orientation", C.c_double * 3),
         ("depth_near", C.c_double), ("depth_far", C.c_double), ("sp_alpha", C.c_float),
         ("seed", C.c_uint64), ("batch_id", C.c_uint32), ("quirks", C.c_int),
-        ("sampler", C.c_int),
+        ("sampler", C.c_int), ("perturbation", C.c_float),
     ]
 
 
@@ -159,6 +159,7 @@ class Oracle:
         p.sp_alpha = sp_alpha
         p.seed, p.batch_id, p.quirks = seed, batch_id, int(quirks)
         p.sampler = int(sampler)
+        p.perturbation = 0.0
         self.p = p
         self.half_window = half_window
         self.sum_i, self.sum_ii = box_moments(self.ref, half_window, fp32)
@@ -245,6 +246,8 @@ def from_images(images, ref_id: int, params, source_texels=None, ref_texels=None
 
     ref_t = ref_texels if ref_texels is not None else texels(ref_im)
     src_t = source_texels if source_texels is not None else [texels(s) for s in srcs]
-    return Oracle(ref_t, src_t, np.array(hh), ik, params.half_window, params.depth_near, params.depth_far,
-                  params.sp_alpha, params.seed, (params.orientation_x, 0.0, params.orientation_z),
-                  bool(params.quirks), 0, fp32, getattr(params, "sampler", 0))
+    orc = Oracle(ref_t, src_t, np.array(hh), ik, params.half_window, params.depth_near, params.depth_far,
+                 params.sp_alpha, params.seed, (params.orientation_x, 0.0, params.orientation_z),
+                 bool(params.quirks), 0, fp32, getattr(params, "sampler", 0))
+    orc.p.perturbation = float(getattr(params, "perturbation", 0.0))
+    return orc

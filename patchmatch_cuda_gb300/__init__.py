@@ -22,13 +22,14 @@ import numpy as np
 from . import _native
 from ._native import (DIR_BOTTOM_TO_TOP, DIR_LEFT_TO_RIGHT, DIR_RIGHT_TO_LEFT, DIR_TOP_TO_BOTTOM,
                       PRECISION_FP32, PRECISION_MIXED, PREFILTER_BOX, PREFILTER_GAUSSIAN,
-                      PREFILTER_NONE, PatchMatchError, PmParams, PmStats, PmView)
+                      PREFILTER_NONE, INIT_PROPOSAL, INIT_RANDOM, PatchMatchError, PmParams, PmStats,
+                      PmView)
 
 __all__ = [
     "Image", "PatchMatch", "Engine", "read_middlebury", "read_pnm", "write_pgm", "default_params",
     "load_depth_file", "PatchMatchError", "PREFILTER_NONE", "PREFILTER_BOX", "PREFILTER_GAUSSIAN",
     "PRECISION_FP32", "PRECISION_MIXED", "DIR_LEFT_TO_RIGHT", "DIR_TOP_TO_BOTTOM",
-    "DIR_RIGHT_TO_LEFT", "DIR_BOTTOM_TO_TOP",
+    "DIR_RIGHT_TO_LEFT", "DIR_BOTTOM_TO_TOP", "INIT_RANDOM", "INIT_PROPOSAL",
 ]
 
 
@@ -197,6 +198,22 @@ class Engine:
 
     def save_depth(self, path) -> None:
         self._chk(self._lib.pm_save_depth(self.h, str(path).encode()))
+
+    def proposal_shape(self) -> tuple:
+        """(height, width) of the learned proposal's network input for this reference."""
+        hh, ww = C.c_int(), C.c_int()
+        self._chk(self._lib.pm_proposal_input(self.h, None, C.byref(hh), C.byref(ww)))
+        return hh.value, ww.value
+
+    def proposal_input(self, d_out: int) -> None:
+        """Writes the network input (FP32 [height][width][17]) to DEVICE address d_out."""
+        self._chk(self._lib.pm_proposal_input(self.h, C.c_void_p(d_out), None, None))
+
+    def set_proposal(self, net) -> None:
+        """Attaches a proposal network (patchmatch_cuda_gb300.proposal.ProposalNet sized for
+        this reference, batch 1) used by runs with init_mode = INIT_PROPOSAL; None detaches."""
+        self._proposal = net
+        self._chk(self._lib.pm_set_proposal(self.h, net.h if net is not None else None))
 
     def stats(self) -> PmStats:
         s = PmStats()

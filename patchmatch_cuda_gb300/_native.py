@@ -24,6 +24,7 @@ PREFILTER_NONE, PREFILTER_BOX, PREFILTER_GAUSSIAN = 0, 1, 2
 PRECISION_FP32, PRECISION_MIXED = 0, 1
 SAMPLER_EXACT, SAMPLER_HARDWARE = 0, 1
 TEXELS_AUTO, TEXELS_U8, TEXELS_F16, TEXELS_F32 = 0, 1, 2, 4
+INIT_RANDOM, INIT_PROPOSAL = 0, 1
 DIR_LEFT_TO_RIGHT, DIR_TOP_TO_BOTTOM, DIR_RIGHT_TO_LEFT, DIR_BOTTOM_TO_TOP = 0, 1, 2, 3
 
 # Every symbol include/patchmatch_gb300.h declares.
@@ -34,6 +35,9 @@ EXPORTED_SYMBOLS = [
     "pm_compute_costs", "pm_run_sweep", "pm_set_depth", "pm_get_costs", "pm_set_costs",
     "pm_get_ref_maps", "pm_get_source_texels", "pm_eval_costs", "pm_sample_source",
     "pm_transpose_layers", "pm_philox", "pm_box_moments_noalloc", "pm_check_reciprocal",
+    "pm_gemm_bf16", "pm_gemm_error", "pm_net_create", "pm_net_destroy", "pm_net_num_params",
+    "pm_net_get_params", "pm_net_set_params", "pm_net_forward", "pm_net_gradients", "pm_net_train_step",
+    "pm_net_layout", "pm_net_size", "pm_set_proposal", "pm_proposal_input",
 ]
 
 
@@ -52,7 +56,8 @@ class PmParams(C.Structure):
         ("orientation_z", C.c_float), ("seed", C.c_uint64), ("precision", C.c_int),
         ("init_mode", C.c_int), ("threads_per_line", C.c_int), ("quirks", C.c_int),
         ("gpu_id", C.c_int), ("block_dim_x", C.c_int), ("block_dim_y", C.c_int),
-        ("sampler", C.c_int), ("texel_format", C.c_int),
+        ("sampler", C.c_int), ("texel_format", C.c_int), ("num_sweeps", C.c_int),
+        ("proposal_threshold", C.c_float), ("perturbation", C.c_float),
     ]
 
 
@@ -112,6 +117,21 @@ def load_engine() -> C.CDLL:
         "pm_transpose_layers": (C.c_int, [P, C.c_size_t, P, C.c_size_t, C.c_int, C.c_int, C.c_int, P]),
         "pm_philox": (C.c_int, [C.c_uint64, C.c_int, P, P]),
         "pm_check_reciprocal": (C.c_int, [C.c_int, P]),
+        "pm_gemm_bf16": (C.c_int, [P, C.c_int, P, C.c_int, C.c_int, C.c_int, C.c_int, P, C.c_int, C.c_int, P,
+                                   C.c_int, C.c_int, P]),
+        "pm_gemm_error": (C.c_int, [P, C.c_int]),
+        "pm_net_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_uint64, P]),
+        "pm_net_destroy": (C.c_int, [P]),
+        "pm_net_num_params": (C.c_int, [P, P]),
+        "pm_net_get_params": (C.c_int, [P, P, C.c_size_t]),
+        "pm_net_set_params": (C.c_int, [P, P, C.c_size_t]),
+        "pm_net_forward": (C.c_int, [P, P, P, P]),
+        "pm_net_gradients": (C.c_int, [P, P, P, C.c_float, C.c_float, P, C.c_size_t, P]),
+        "pm_net_train_step": (C.c_int, [P, P, P, C.c_float, C.c_float, C.c_float, P]),
+        "pm_net_layout": (C.c_int, [P, P, P, C.c_int]),
+        "pm_net_size": (C.c_int, [P, P, P, P]),
+        "pm_set_proposal": (C.c_int, [H, P]),
+        "pm_proposal_input": (C.c_int, [H, P, P, P]),
         "pm_box_moments_noalloc": (C.c_int, [P, C.c_size_t, C.c_int, C.c_int, C.c_int, P, P, P, C.c_size_t, P]),
     }
     for name, (res, args) in sig.items():

@@ -6,6 +6,7 @@
 // source view, and a CUDA graph of the whole run schedule, captured on first use.
 #include <cuda_fp16.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -44,6 +45,12 @@ struct pm_handle {
     SweepArgs *h_sweep_args = nullptr;   // pinned, one per sweep of the schedule
 
     int wpl[2] = {0, 0};                // warps per line: [vertical sweeps, horizontal sweeps]
+    // learned proposal
+    pm_net *net = nullptr;
+    ProposalGeom geom{};
+    int prop_src[2] = {0, 0};           // the two sources nearest to the reference camera
+    float *d_quarter[3] = {nullptr, nullptr, nullptr};  // reference, source 0, source 1
+    float *d_prop_in = nullptr, *d_prop_out = nullptr;
     cudaGraphExec_t graph = nullptr;
     bool ran = false;
     pm_stats stats{};
@@ -237,6 +244,7 @@ void fill_sweep_args(SweepArgs &a, const RefDesc *refs, const int *lines, int nr
     a.sweep_id = sweep_id;
     a.num_samples = num_samples;
     a.record_views = record;
+    a.perturb = 0.0f;
     a.line_start[0] = 0;
     for (int i = 0; i < nrefs; ++i) a.line_start[i + 1] = a.line_start[i] + lines[i];
     a.total_lines = a.line_start[nrefs];
@@ -291,24 +299,55 @@ int lines_of(const pm_handle *h, int dir)
 }
 
 // The whole run: initial depth, initial costs, iterations x 4 sweeps (patchMatch.cu:307-394).
+// Half-width of the local random search in sweep k: perturbation x 2^(-k/4) (0: the
+// reference's uniform search only).
+float sweep_perturb(const pm_handle *h, int k)
+{
+    return h->p.perturbation > 0.0f ? h->p.perturbation * std::exp2(-0.25f * (float)k) : 0.0f;
+}
+
+// Sweeps the schedule runs: num_iterations x 4, or fewer when num_sweeps says so.
+int schedule_sweeps(const pm_handle *h)
+{
+    const int all = 4 * h->p.num_iterations;
+    return h->p.num_sweeps > 0 && h->p.num_sweeps < all ? h->p.num_sweeps : all;
+}
+
+// Learned initialisation on stream s: plane-sweep input, network, depth from its output.
+cudaError_t enqueue_proposal_init(pm_handle *h, cudaStream_t s)
+{
+    if (!h->net || !h->d_prop_in) return cudaErrorInvalidValue;
+    const ProposalGeom &g = h->geom;
+    cudaError_t e = launch_sweep_input(g, h->d_quarter[0], h->d_quarter[1], h->d_quarter[2], h->d_prop_in, s);
+    if (e != cudaSuccess) return e;
+    if (pm_net_forward(h->net, h->d_prop_in, h->d_prop_out, s) != PM_OK) return cudaErrorLaunchFailure;
+    return launch_proposal_init(h->d_desc, 0, h->W * h->H, g, h->d_prop_out, h->p.proposal_threshold, s);
+}
+
+// The whole run: initial depth, initial costs, iterations x 4 sweeps (patchMatch.cu:307-394).
 cudaError_t enqueue_schedule(pm_handle *h)
 {
     cudaError_t e = cudaMemsetAsync(h->d_evals, 0, 2 * sizeof(unsigned long long), h->stream);
     if (e != cudaSuccess) return e;
-    e = launch_init_depth(h->d_desc, 0, h->W * h->H, h->stream);
+    if (h->p.init_mode == PM_INIT_PROPOSAL) e = enqueue_proposal_init(h, h->stream);
+    else e = launch_init_depth(h->d_desc, 0, h->W * h->H, h->stream);
     if (e != cudaSuccess) return e;
     e = enqueue_costs(h, 1);
     if (e != cudaSuccess) return e;
-    const int iters = h->p.num_iterations;
-    for (int it = 0; it < iters; ++it)
-        for (int d = 0; d < 4; ++d) {
-            SweepArgs &a = h->h_sweep_args[4 * it + d];
-            const int lines = lines_of(h, d);
-            fill_sweep_args(a, h->d_desc, &lines, 1, d, (uint32_t)(4 * it + d), it == 0 ? 1 : 0,
-                            (it == iters - 1 && d == PM_DIR_BOTTOM_TO_TOP) ? 1 : 0);
-            e = enqueue_sweep(window_side(h), hw_of(h), h->wpl[orient(d)], a, h->stream);
-            if (e != cudaSuccess) return e;
-        }
+    const int nsweeps = schedule_sweeps(h);
+    for (int k = 0; k < nsweeps; ++k) {
+        const int it = k / 4, d = k % 4;
+        SweepArgs &a = h->h_sweep_args[k];
+        const int lines = lines_of(h, d);
+        // the first iteration samples one view after a random initialisation
+        // (patchMatch.cu:307-316); a learned initialisation starts with meaningful costs and
+        // samples numOfSamples from the start
+        const int s_first = h->p.init_mode == PM_INIT_RANDOM ? 1 : 0;
+        fill_sweep_args(a, h->d_desc, &lines, 1, d, (uint32_t)k, it == 0 ? s_first : 0, k == nsweeps - 1 ? 1 : 0);
+        a.perturb = sweep_perturb(h, k);
+        e = enqueue_sweep(window_side(h), hw_of(h), h->wpl[orient(d)], a, h->stream);
+        if (e != cudaSuccess) return e;
+    }
     return cudaSuccess;
 }
 
@@ -403,6 +442,9 @@ void pm_default_params(pm_params *p)
     p->seed = 0x5EEDull;
     p->precision = PM_PRECISION_FP32;
     p->init_mode = PM_INIT_RANDOM;
+    p->num_sweeps = 0;
+    p->proposal_threshold = 0.5f;
+    p->perturbation = 0.0f;
     p->threads_per_line = 0;
     p->quirks = 1;
     p->sampler = PM_SAMPLER_HARDWARE;
@@ -433,7 +475,8 @@ pm_status pm_destroy(pm_handle *h)
     if (h->tex_layered) cudaDestroyTextureObject(h->tex_layered);
     if (h->layered) release_array(h->device, h->layer_w, h->layer_h, h->texel_bytes, h->layered, h->V);
     void *bufs[] = {h->d_ref, h->d_sum_i, h->d_sum_ii, h->d_c1, h->d_depth, h->d_cost, h->d_beta,
-                    h->d_view_sel, h->d_evals, h->d_hh, h->d_hh64, h->d_desc};
+                    h->d_view_sel, h->d_evals, h->d_hh, h->d_hh64, h->d_desc, h->d_quarter[0],
+                    h->d_quarter[1], h->d_quarter[2], h->d_prop_in, h->d_prop_out};
     for (void *b : bufs)
         if (b) cudaFreeAsync(b, h->stream);
     if (h->stream) {
@@ -464,7 +507,9 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
         p.prefilter < PM_PREFILTER_NONE || p.prefilter > PM_PREFILTER_GAUSSIAN ||
         (p.prefilter == PM_PREFILTER_GAUSSIAN && !(p.gaussian_sigma > 0.0f)) ||
         (p.precision != PM_PRECISION_FP32 && p.precision != PM_PRECISION_MIXED) ||
-        p.init_mode != PM_INIT_RANDOM ||
+        (p.init_mode != PM_INIT_RANDOM && p.init_mode != PM_INIT_PROPOSAL) || p.num_sweeps < 0 ||
+        !(p.proposal_threshold >= 0.0f && p.proposal_threshold <= 1.0f) ||
+        !(p.perturbation >= 0.0f && p.perturbation < 1.0f) ||
         (p.sampler != PM_SAMPLER_EXACT && p.sampler != PM_SAMPLER_HARDWARE) ||
         (p.texel_format != PM_TEXELS_AUTO && p.texel_format != PM_TEXELS_U8 &&
          p.texel_format != PM_TEXELS_F16 && p.texel_format != PM_TEXELS_F32) ||
@@ -522,6 +567,48 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
         h->src_h[si] = views[i].height;
         ++si;
     }
+    // proposal: the two sources whose camera centres are nearest the reference's, and their
+    // homographies for fronto-parallel planes
+    {
+        auto centre = [](const pm_view &v, double c[3]) {
+            for (int i = 0; i < 3; ++i)
+                c[i] = -((double)v.R[i] * v.t[0] + (double)v.R[3 + i] * v.t[1] + (double)v.R[6 + i] * v.t[2]);
+        };
+        double cr[3];
+        centre(ref, cr);
+        std::vector<std::pair<double, int>> dist;
+        int k = 0;
+        for (int i = 0; i < n_views; ++i) {
+            if (i == ref_id) continue;
+            double c[3];
+            centre(views[i], c);
+            dist.push_back({(c[0] - cr[0]) * (c[0] - cr[0]) + (c[1] - cr[1]) * (c[1] - cr[1]) +
+                                (c[2] - cr[2]) * (c[2] - cr[2]),
+                            k++});
+        }
+        std::sort(dist.begin(), dist.end());
+        h->prop_src[0] = dist[0].second;
+        h->prop_src[1] = dist.size() > 1 ? dist[1].second : dist[0].second;
+        ProposalGeom &g = h->geom;
+        g.w4 = h->W / 4;
+        g.h4 = h->H / 4;
+        g.wp = (g.w4 + 15) / 16 * 16;
+        g.hp = (g.h4 + 15) / 16 * 16;
+        g.inv_far = 1.0f / p.depth_far;
+        g.inv_range = 1.0f / p.depth_near - 1.0f / p.depth_far;
+        for (int j = 0; j < 2; ++j) {
+            int vi = -1;
+            for (int i = 0, s2 = 0; i < n_views; ++i) {
+                if (i == ref_id) continue;
+                if (s2++ == h->prop_src[j]) vi = i;
+            }
+            double o[18];
+            relative_homographies(ref, kr_inv, views[vi], 0.0, 1.0, o);
+            for (int q = 0; q < 18; ++q) g.hh[j][q] = (float)o[q];
+            g.sw4[j] = views[vi].width / 4;
+            g.sh4[j] = views[vi].height / 4;
+        }
+    }
 
     pm_status st = set_device(h);
     if (st != PM_OK) { pm_destroy(h); return st; }
@@ -556,6 +643,11 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
     PM_TRY(dalloc(&h->d_hh, hh.size() * 4, s));
     PM_TRY(dalloc(&h->d_hh64, hh64.size() * 8, s));
     PM_TRY(dalloc(&h->d_desc, sizeof(RefDesc), s));
+    if (h->geom.w4 > 0 && h->geom.h4 > 0) {
+        PM_TRY(dalloc(&h->d_quarter[0], (size_t)h->geom.w4 * h->geom.h4 * 4 + 16, s));
+        for (int j = 0; j < 2; ++j)
+            PM_TRY(dalloc(&h->d_quarter[1 + j], (size_t)std::max(1, h->geom.sw4[j] * h->geom.sh4[j]) * 4 + 16, s));
+    }
     PM_TRY(cudaMemsetAsync(h->d_view_sel, 255, npix * (size_t)p.num_samples, s));
     PM_TRY(cudaMemsetAsync(h->d_evals, 0, 2 * sizeof(unsigned long long), s));
     PM_TRY(cudaMemcpyAsync(h->d_hh, hh.data(), hh.size() * 4, cudaMemcpyHostToDevice, s));
@@ -594,6 +686,13 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
         PM_TRY(cudaMemcpy2DAsync(d_u8, (size_t)v.width, v.gray, (size_t)v.stride, (size_t)v.width,
                                  (size_t)v.height, cudaMemcpyHostToDevice, s));
         const bool is_ref = i == ref_id;
+        if (h->d_quarter[0]) {
+            const int sidx = is_ref ? -1 : (i < ref_id ? i : i - 1);
+            if (is_ref) PM_TRY(launch_quarter(d_u8, v.width, h->geom.w4, h->geom.h4, h->d_quarter[0], s));
+            for (int j = 0; j < 2; ++j)
+                if (!is_ref && sidx == h->prop_src[j])
+                    PM_TRY(launch_quarter(d_u8, v.width, h->geom.sw4[j], h->geom.sh4[j], h->d_quarter[1 + j], s));
+        }
         float *texels = is_ref && !filtered ? h->d_ref : d_f0;
         PM_TRY(launch_u8_to_float(d_u8, v.width, texels, v.width, v.height, s));
         if (filtered) {
@@ -725,6 +824,8 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
 pm_status pm_run_async(pm_handle *h)
 {
     if (!h) return PM_ERR_INVALID_ARGUMENT;
+    if (h->p.init_mode == PM_INIT_PROPOSAL && !h->net)
+        return fail(h, PM_ERR_STATE, "init_mode is PM_INIT_PROPOSAL but no network is attached");
     pm_status st = set_device(h);
     if (st != PM_OK) return st;
     if (!h->graph) {
@@ -797,13 +898,14 @@ pm_status pm_run_batch(pm_handle *const *hs, int n)
             const int m = (int)std::min<size_t>(MAX_BATCH_REFS, grp.size() - start);
             RefDesc *d_descs = nullptr;
             PM_CUDA(h0, cudaMallocAsync((void **)&d_descs, sizeof(RefDesc) * m, s));
-            int max_iters = 0;
+            int max_sweeps = 0;
             for (int i = 0; i < m; ++i) {
                 pm_handle *h = grp[start + i];
                 PM_CUDA(h0, cudaMemcpyAsync(d_descs + i, &h->h_desc, sizeof(RefDesc),
                                             cudaMemcpyHostToDevice, s));
                 PM_CUDA(h0, cudaMemsetAsync(h->d_evals, 0, 2 * sizeof(unsigned long long), s));
-                PM_CUDA(h0, launch_init_depth(d_descs, i, h->W * h->H, s));
+                if (h->p.init_mode == PM_INIT_PROPOSAL) PM_CUDA(h0, enqueue_proposal_init(h, s));
+                else PM_CUDA(h0, launch_init_depth(d_descs, i, h->W * h->H, s));
                 LaunchReq req{};
                 req.kind = LaunchKind::Costs;
                 req.stream = s;
@@ -812,21 +914,25 @@ pm_status pm_run_batch(pm_handle *const *hs, int n)
                 req.axis = 1;
                 req.grid = (h->W * h->H + COST_BLOCK / 32 - 1) / (COST_BLOCK / 32);
                 PM_CUDA(h0, launch_window(h->win, hw_of(h), req));
-                max_iters = std::max(max_iters, h->p.num_iterations);
+                max_sweeps = std::max(max_sweeps, schedule_sweeps(h));
             }
-            std::vector<SweepArgs> args((size_t)max_iters * 4);
-            for (int it = 0; it < max_iters; ++it)
-                for (int d = 0; d < 4; ++d) {
-                    // references still iterating at `it`, in descriptor order
-                    std::vector<int> lines(m, 0);
-                    for (int i = 0; i < m; ++i)
-                        lines[i] = grp[start + i]->p.num_iterations > it ? lines_of(grp[start + i], d) : 0;
-                    // every bottom-to-top sweep records; a reference's last one writes last
-                    SweepArgs &a = args[(size_t)it * 4 + d];
-                    fill_sweep_args(a, d_descs, lines.data(), m, d, (uint32_t)(4 * it + d),
-                                    it == 0 ? 1 : 0, d == PM_DIR_BOTTOM_TO_TOP ? 1 : 0);
-                    PM_CUDA(h0, enqueue_sweep(grp[start]->win, hw_of(grp[start]), batch_wpl(grp[start]->win, hw_of(grp[start]), a.total_lines, h0->device), a, s));
-                }
+            std::vector<SweepArgs> args((size_t)max_sweeps);
+            for (int k = 0; k < max_sweeps; ++k) {
+                const int it = k / 4, d = k % 4;
+                // references still sweeping at k, in descriptor order
+                std::vector<int> lines(m, 0);
+                for (int i = 0; i < m; ++i)
+                    lines[i] = schedule_sweeps(grp[start + i]) > k ? lines_of(grp[start + i], d) : 0;
+                // every sweep records the sampled views; a reference's last one writes last
+                SweepArgs &a = args[(size_t)k];
+                // one view sample in the first iteration after a random initialisation
+                // (patchMatch.cu:307-316); a batch mixing both initialisations follows the first
+                const int s_first = grp[start]->p.init_mode == PM_INIT_RANDOM ? 1 : 0;
+                fill_sweep_args(a, d_descs, lines.data(), m, d, (uint32_t)k, it == 0 ? s_first : 0, 1);
+                a.perturb = sweep_perturb(grp[start], k);
+                PM_CUDA(h0, enqueue_sweep(grp[start]->win, hw_of(grp[start]),
+                                          batch_wpl(grp[start]->win, hw_of(grp[start]), a.total_lines, h0->device), a, s));
+            }
             PM_CUDA(h0, cudaFreeAsync(d_descs, s));
         }
     }
@@ -909,7 +1015,12 @@ pm_status pm_init_depth(pm_handle *h)
     if (!h) return PM_ERR_INVALID_ARGUMENT;
     pm_status st = set_device(h);
     if (st != PM_OK) return st;
-    PM_CUDA(h, launch_init_depth(h->d_desc, 0, h->W * h->H, h->stream));
+    if (h->p.init_mode == PM_INIT_PROPOSAL) {
+        if (!h->net) return fail(h, PM_ERR_STATE, "init_mode is PM_INIT_PROPOSAL but no network is attached");
+        PM_CUDA(h, enqueue_proposal_init(h, h->stream));
+    } else {
+        PM_CUDA(h, launch_init_depth(h->d_desc, 0, h->W * h->H, h->stream));
+    }
     PM_CUDA(h, cudaStreamSynchronize(h->stream));
     return PM_OK;
 }
@@ -934,6 +1045,7 @@ pm_status pm_run_sweep(pm_handle *h, int direction, uint32_t sweep_id, int num_s
     SweepArgs a;
     const int lines = lines_of(h, direction);
     fill_sweep_args(a, h->d_desc, &lines, 1, direction, sweep_id, num_samples, record_views ? 1 : 0);
+    a.perturb = sweep_perturb(h, (int)sweep_id);
     if (record_views && num_samples > h->p.num_samples) return PM_ERR_INVALID_ARGUMENT;
     if (!h->wpl[orient(direction)]) {
         // tune on scratch copies so the caller's state is untouched
@@ -1106,6 +1218,41 @@ pm_status pm_transpose_layers(const float *d_in, size_t in_pitch, float *d_out, 
     cudaError_t e = launch_transpose(d_in, in_pitch, d_out, out_pitch, width, height, layers,
                                      (cudaStream_t)stream);
     if (e != cudaSuccess) { cudaGetLastError(); return PM_ERR_CUDA; }
+    return PM_OK;
+}
+
+pm_status pm_set_proposal(pm_handle *h, pm_net *net)
+{
+    if (!h) return PM_ERR_INVALID_ARGUMENT;
+    if (net) {
+        int b = 0, hh = 0, ww = 0;
+        if (pm_net_size(net, &b, &hh, &ww) != PM_OK || b != 1 || hh != h->geom.hp || ww != h->geom.wp)
+            return fail(h, PM_ERR_INVALID_ARGUMENT, "proposal network size does not match the handle");
+        const pm_status st = set_device(h);
+        if (st != PM_OK) return st;
+        const size_t n = (size_t)h->geom.hp * h->geom.wp;
+        if (!h->d_prop_in) PM_CUDA(h, cudaMalloc((void **)&h->d_prop_in, n * PROPOSAL_IN_CH * sizeof(float)));
+        if (!h->d_prop_out) PM_CUDA(h, cudaMalloc((void **)&h->d_prop_out, n * 2 * sizeof(float)));
+    }
+    if (h->net != net && h->graph) {  // the captured schedule holds the old network's launches
+        cudaGraphExecDestroy(h->graph);
+        h->graph = nullptr;
+    }
+    h->net = net;
+    return PM_OK;
+}
+
+pm_status pm_proposal_input(pm_handle *h, float *d_out, int *height, int *width)
+{
+    if (!h) return PM_ERR_INVALID_ARGUMENT;
+    if (height) *height = h->geom.hp;
+    if (width) *width = h->geom.wp;
+    if (!d_out) return PM_OK;
+    if (!h->d_quarter[0]) return fail(h, PM_ERR_UNSUPPORTED, "image smaller than 4 x 4");
+    const pm_status st = set_device(h);
+    if (st != PM_OK) return st;
+    PM_CUDA(h, launch_sweep_input(h->geom, h->d_quarter[0], h->d_quarter[1], h->d_quarter[2], d_out, h->stream));
+    PM_CUDA(h, cudaStreamSynchronize(h->stream));
     return PM_OK;
 }
 

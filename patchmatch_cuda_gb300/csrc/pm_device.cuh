@@ -81,6 +81,16 @@ __device__ __forceinline__ float draw_uniform(uint64_t seed, uint32_t pixel, uin
     return (float)((o.x >> 8) + 1u) * (1.0f / 16777216.0f);
 }
 
+// The same counter's first two words as uniforms in (0, 1]: (x, y).
+__device__ __forceinline__ float2 draw_uniform2(uint64_t seed, uint32_t pixel, uint32_t sweep,
+                                                uint32_t purpose, uint32_t sub, uint32_t batch)
+{
+    const uint4 o = philox4x32_10(make_uint4(pixel, sweep, (purpose << 16) | sub, batch),
+                                  make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)));
+    return make_float2((float)((o.x >> 8) + 1u) * (1.0f / 16777216.0f),
+                       (float)((o.y >> 8) + 1u) * (1.0f / 16777216.0f));
+}
+
 // ---- source fetch --------------------------------------------------------------------------
 // The reference samples tex2DLayered(src, u/z + 0.5, v/z + 0.5) with linear filtering and a
 // zero border (patchMatch.cu:543): bilinear interpolation at (u/z, v/z) with texel i at

@@ -71,4 +71,31 @@ cudaError_t launch_philox(uint64_t seed, int n, const uint32_t *ctr, uint32_t *o
                           cudaStream_t s);
 cudaError_t launch_check_rcp(int exp_shift, unsigned long long *mismatches, cudaStream_t s);
 
+// Learned proposal (pm_proposal.cu): quarter-resolution images, the plane-sweep input of the
+// network (17 channels), and the initial depth from its output.
+constexpr int PROPOSAL_IN_CH = 17;
+constexpr int PROPOSAL_PLANES = 8;
+struct ProposalGeom {
+    int w4, h4;          // quarter-resolution reference size
+    int wp, hp;          // network size (w4, h4 rounded up to multiples of 16)
+    int sw4[2], sh4[2];  // quarter-resolution size of the two sources
+    float inv_far, inv_range;
+    float hh[2][18];     // H1, H2 of the two sources for the plane normal (0, 0, 1)
+};
+cudaError_t launch_quarter(const uint8_t *img, int pitch, int w4, int h4, float *out, cudaStream_t s);
+cudaError_t launch_sweep_input(const ProposalGeom &g, const float *ref_q, const float *src0, const float *src1,
+                               float *out, cudaStream_t s);
+cudaError_t launch_proposal_init(const RefDesc *refs, int r, int npix, const ProposalGeom &g, const float *prob,
+                                 float threshold, cudaStream_t s);
+
+// BF16 tensor-core GEMM C[M, N] (+)= A[M, K] . B[N, K]^T (pm_gemm.cu). M % 128 == 0,
+// N % 16 == 0, K % 64 == 0, leading dimensions multiples of 8 elements, 16-byte aligned
+// pointers. splits > 1 (GEMM_ATOMIC_F32 only) divides K over the grid. *err is set to 1 if a
+// CTA's pipeline wait times out.
+enum GemmMode { GEMM_STORE_BF16 = 0, GEMM_STORE_F32 = 1, GEMM_ATOMIC_F32 = 2 };
+cudaError_t gemm_prepare();  // one-time host set-up; call before capturing GEMMs in a graph
+cudaError_t launch_gemm_bf16(const void *A, int lda, const void *B, int ldb, int M, int N, int K,
+                             void *C, int ldc, int mode, const float *bias, int relu, int splits,
+                             unsigned *err, cudaStream_t s);
+
 }  // namespace pm

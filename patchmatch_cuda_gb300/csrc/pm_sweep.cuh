@@ -29,6 +29,7 @@ struct SweepArgs {
     uint32_t sweep_id;
     int num_samples;                     // > 0 overrides the descriptors' (iteration 0: 1)
     int record_views;
+    float perturb;                       // > 0: local random search of half-width perturb
     int line_start[MAX_BATCH_REFS + 1];  // prefix sums of lines per reference
 };
 
@@ -63,7 +64,8 @@ struct StepCtl {
 // The cost-2 replacement draws are made by warp 0 when a cost of 2 occurs.
 struct StepDraws {
     float sample[MAX_VIEWS];  // view samples (RNG_SAMPLE)
-    float depth;              // random depth (RNG_RAND_DEPTH)
+    float depth;              // random depth (RNG_RAND_DEPTH, first word)
+    float mode;               // local or global random search (RNG_RAND_DEPTH, second word)
 };
 
 __device__ __forceinline__ void make_draws(const RefDesc &D, uint32_t pix, uint32_t sweep, int S,
@@ -74,12 +76,20 @@ __device__ __forceinline__ void make_draws(const RefDesc &D, uint32_t pix, uint3
     // lanes below S draw the view samples; the last lane the random depth (when S < 32)
     const bool depth_lane = lane == 31 && S < 32;
     if (lane < S || depth_lane) {
-        const float u = draw_uniform(seed, pix, sweep, depth_lane ? RNG_RAND_DEPTH : RNG_SAMPLE,
-                                     depth_lane ? 0 : lane, batch);
-        if (depth_lane) out.depth = u;
-        else out.sample[lane] = u;
+        const float2 u = draw_uniform2(seed, pix, sweep, depth_lane ? RNG_RAND_DEPTH : RNG_SAMPLE,
+                                       depth_lane ? 0 : lane, batch);
+        if (depth_lane) {
+            out.depth = u.x;
+            out.mode = u.y;
+        } else {
+            out.sample[lane] = u.x;
+        }
     }
-    if (S >= 32 && lane == 0) out.depth = draw_uniform(seed, pix, sweep, RNG_RAND_DEPTH, 0, batch);
+    if (S >= 32 && lane == 0) {
+        const float2 u = draw_uniform2(seed, pix, sweep, RNG_RAND_DEPTH, 0, batch);
+        out.depth = u.x;
+        out.mode = u.y;
+    }
 }
 
 // One directional sweep. One CTA per line of `blockDim.x / 32` warps. Warp 0 owns the line's
@@ -250,7 +260,14 @@ __global__ void __maxnreg__(SweepRegs<HW>::value) sweep_kernel(const __grid_cons
             }
             cdf = cdf / __shfl_sync(FULL_MASK, cdf, V - 1);
             // random depth and view samples, first view with u <= CDF (:937-961)
-            const float d_rand = fmaf(dr.depth, D.depth_span, D.depth_near);
+            // the random hypothesis: uniform in [near, far] (patchMatch.cu:937); with a local
+            // search (no counterpart in the reference) half of the pixels instead draw within
+            // +-perturb (relative) of their current depth
+            float d_rand = fmaf(dr.depth, D.depth_span, D.depth_near);
+            if (A.perturb > 0.0f && dr.mode >= 0.5f)
+                d_rand = fminf(fmaxf(__fmul_rn(d_cur, fmaf(A.perturb, fmaf(2.0f, dr.depth, -1.0f), 1.0f)),
+                                     D.depth_near),
+                               D.depth_near + D.depth_span);
             const float u_mine = lane < S ? dr.sample[lane] : 2.0f;
             StepCtl &C = s_ctl[buf];
             unsigned umask = 0;

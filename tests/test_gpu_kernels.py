@@ -316,3 +316,30 @@ def test_full_run_matches_oracle(small_scene, sampler, parity_log):
     st = eng.stats()
     assert st.cost_evals > 0
     eng.close()
+
+
+@pytest.mark.parametrize("direction", [1, 2])
+def test_sweep_lockstep_local_search(small_scene, direction, parity_log):
+    """The local random search (perturbation > 0, no counterpart in the reference) against the
+    oracle's restatement of it: same decisions and costs as the plain lockstep test."""
+    eng = make_engine(small_scene, perturbation=0.05)
+    orc = oracle_for(eng, small_scene)
+    assert abs(orc.p.perturbation - 0.05) < 1e-7
+    eng.init_depth()
+    eng.compute_costs(1)
+    d0 = eng.depth().astype(np.float64)
+    c0 = eng.costs().astype(np.float64)
+    S = small_scene.workload.num_samples
+    eng.run_sweep(direction, 4 + direction, S)
+    gd, gc = eng.depth(), eng.costs()
+    od, oc = d0.copy(), c0.copy()
+    orc.sweep(od, oc, direction, 4 + direction, S)
+    prefix, nsteps = first_divergence(gd, od, direction)
+    events = int(np.sum(prefix < nsteps))
+    decisions = int(np.sum(np.minimum(prefix + 1, nsteps)))
+    changed = float(np.mean(np.abs(gd - d0) > 1e-6 * d0))
+    parity_log(f"sweep_lockstep_local_search_dir{direction}", divergence_events=events, decisions=decisions,
+               changed_fraction=changed)
+    assert events / decisions <= 2e-4, f"{events} divergences in {decisions} decisions"
+    assert changed > 0.05
+    eng.close()
