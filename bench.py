@@ -48,6 +48,8 @@ def parse_args():
     ap.add_argument("--profile", type=int, default=None, metavar="DIR",
                     help="run only the initial state and one sweep in direction DIR (for ncu)")
     ap.add_argument("--threads-per-line", type=int, default=0)
+    ap.add_argument("--profile-net", action="store_true",
+                    help="run only the proposal network's forward pass on the workload (for ncu)")
     return ap.parse_args()
 
 
@@ -64,6 +66,27 @@ def run_profile(args):
     st = eng.stats()
     print(json.dumps({"sweep_ms": st.ms_sweeps, "cost_evals": st.cost_evals,
                       "threads_per_line": st.threads_per_line}))
+    eng.close()
+    return 0
+
+
+def run_profile_net(args):
+    """The proposal network's forward pass on the workload's plane-sweep input, 5 times."""
+    import torch
+    from patchmatch_cuda_gb300 import Engine, proposal, scene
+    wl = scene.WORKLOADS[args.workload]
+    sv = scene.make_views(wl)
+    eng = Engine(sv.images, sv.ref_id, wl.params())
+    net = proposal.for_engine(eng)
+    hp, wp = eng.proposal_shape()
+    x = torch.empty((hp, wp, 17), device="cuda")
+    y = torch.empty((hp, wp, 2), device="cuda")
+    eng.proposal_input(x.data_ptr())
+    for _ in range(5):
+        net.forward(x.data_ptr(), y.data_ptr())
+    torch.cuda.synchronize()
+    print(json.dumps({"net_input": [hp, wp, 17], "gflop_per_forward": proposal.forward_flops(hp, wp) / 1e9}))
+    net.close()
     eng.close()
     return 0
 
@@ -362,6 +385,7 @@ def run_ours(args):
         variants[name] = {"ms_per_depth_map": st.ms_total, "g_cost_evals_per_s": st.cost_evals / st.ms_total / 1e6,
                           "bad_pixel_pct_1pct": round(100 * scene.bad_pixel_rate(ev.depth(), sv.gt_depth), 3)}
         ev.close()
+    learned = learned_vs_plain(sv, wl, local, flush, max(args.steps, 3))
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(eng, sv, wl, args.cpu_seconds)
@@ -401,6 +425,7 @@ def run_ours(args):
             "e2e": {"value": e2e_value, "unit": "G cost-evals/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_max / args.steps},
             "variants": variants,
+            "learned_vs_plain": learned,
             "gpu_launches": launches_per_map * args.steps,
             "clocks": clocks.summary(),
         }
@@ -409,6 +434,78 @@ def run_ours(args):
         import torch.distributed as dist
         dist.destroy_process_group()
     return 0
+
+
+def _timed_runs(eng, flush, reps):
+    """Median ms of `reps` depth maps on the engine's stream (L2 flushed before each)."""
+    import torch
+    stream = torch.cuda.ExternalStream(eng.stream())
+    eng.run()
+    ms = []
+    for _ in range(reps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        eng.run_async()
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    return statistics.median(ms)
+
+
+def learned_vs_plain(sv, wl, device, flush, reps):
+    """The learned proposal against plain PatchMatch on the same reference: ms per depth map
+    (end of upload to depth ready, inputs resident) and bad-pixel rate against ground truth,
+    plus the network's forward pass against the BF16 tensor peak (2 FLOP per MAC)."""
+    import torch
+    from patchmatch_cuda_gb300 import INIT_PROPOSAL, Engine, proposal, scene
+    if not proposal.WEIGHTS.exists():
+        return None
+    out = {}
+    runs = [("plain_20_sweeps", dict()),
+            ("learned_4_sweeps", dict(init_mode=INIT_PROPOSAL, num_sweeps=4, perturbation=0.05)),
+            ("learned_8_sweeps", dict(init_mode=INIT_PROPOSAL, num_sweeps=8, perturbation=0.05))]
+    params = proposal.load_params()
+    net_ms = gflop = None
+    for name, over in runs:
+        e = Engine(sv.images, sv.ref_id, wl.params(gpu_id=device, **over))
+        net = proposal.for_engine(e, params) if over else None
+        ms = _timed_runs(e, flush, reps)
+        out[name] = {"ms_per_depth_map": round(ms, 3),
+                     "bad_pixel_pct_1pct": round(100 * scene.bad_pixel_rate(e.depth(), sv.gt_depth), 3),
+                     "sweeps": 4 * wl.iterations if not over else over["num_sweeps"],
+                     "cost_evals": e.stats().cost_evals}
+        if net is not None and net_ms is None:
+            # the network alone: forward of the 17-channel plane-sweep input
+            hp, wp = e.proposal_shape()
+            x = torch.empty((hp, wp, 17), device="cuda")
+            y = torch.empty((hp, wp, 2), device="cuda")
+            e.proposal_input(x.data_ptr())
+            for _ in range(3):
+                net.forward(x.data_ptr(), y.data_ptr())
+            t = []
+            for _ in range(10):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                net.forward(x.data_ptr(), y.data_ptr(), torch.cuda.current_stream().cuda_stream)
+                e1.record()
+                e1.synchronize()
+                t.append(e0.elapsed_time(e1))
+            net_ms = statistics.median(t)
+            gflop = proposal.forward_flops(hp, wp) / 1e9
+        e.close()
+        if net is not None:
+            net.close()
+    base = out["plain_20_sweeps"]["ms_per_depth_map"]
+    for name, _ in runs[1:]:
+        out[name]["speedup_vs_plain"] = round(base / out[name]["ms_per_depth_map"], 3)
+    peak = float(measured_peaks().get("bf16_tflops", 1900.0))
+    tflops = gflop / net_ms if net_ms else None
+    out["network_forward"] = {"ms": round(net_ms, 4), "gflop": round(gflop, 3), "tflops": round(tflops, 3),
+                              "peak_tflops": peak, "frac_of_bf16_peak": round(tflops / peak, 5),
+                              "peak_source": "MEASURED_PEAKS.json bf16_tflops (cuBLAS burst)"}
+    return out
 
 
 def run_batched(args):
@@ -461,6 +558,8 @@ def main():
         return run_batched(args)
     if args.profile is not None:
         return run_profile(args)
+    if args.profile_net:
+        return run_profile_net(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

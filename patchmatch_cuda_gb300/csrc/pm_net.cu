@@ -60,6 +60,18 @@ __global__ void im2col_kernel(const bf16 *__restrict__ in, int cs, int co, int C
     const int p = (int)(i / chunks), k0 = (int)(i % chunks) * 8;
     const int b = p / (Ho * Wo), r = p % (Ho * Wo), oy = r / Wo, ox = r % Wo;
     const int pad = (ksize - 1) / 2, K = ksize * ksize * C;
+    if ((C & 7) == 0 && (cs & 7) == 0 && (co & 7) == 0) {
+        // the 8 elements are 8 consecutive channels of one tap: one 16-byte load
+        uint4 w = make_uint4(0, 0, 0, 0);
+        if (k0 < K) {
+            const int t = k0 / C, c = k0 % C;
+            const int iy = oy * stride + t / ksize - pad, ix = ox * stride + t % ksize - pad;
+            if (iy >= 0 && iy < H && ix >= 0 && ix < W)
+                w = *(const uint4 *)(in + ((size_t)(b * H + iy) * W + ix) * cs + co + c);
+        }
+        *(uint4 *)(col + (size_t)p * Kpad + k0) = w;
+        return;
+    }
     __align__(16) bf16 v[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) {

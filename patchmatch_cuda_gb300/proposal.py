@@ -87,6 +87,33 @@ class ProposalNet:
         np.savez_compressed(path, params=self.params(), meta=json.dumps(meta))
 
 
+WIDTHS = (32, 64, 96, 128, 128)
+
+
+def layer_table():
+    """(cin, cout, ksize, stride, relu, input level) of the network's convolutions in execution
+    order, as pm_net.cu builds them."""
+    c = WIDTHS
+    up = (c[1], c[2], c[3], c[4])
+    t = [(IN_CH, c[0], 3, 1, 1, 0), (c[0], c[0], 3, 1, 1, 0)]
+    for lv in range(1, 4):
+        t += [(c[lv - 1], c[lv], 3, 2, 1, lv - 1), (c[lv], c[lv], 3, 1, 1, lv)]
+    t += [(c[3], c[4], 3, 2, 1, 3), (c[4], c[4], 3, 1, 1, 4)]
+    for lv in range(3, -1, -1):
+        t += [(up[lv] + c[lv], c[lv], 3, 1, 1, lv), (c[lv], c[lv], 3, 1, 1, lv)]
+    t.append((c[0], 2, 1, 1, 0, 0))
+    return t
+
+
+def forward_flops(height: int, width: int, batch: int = 1) -> float:
+    """2 x multiply-accumulates of one forward pass (unpadded channels and taps)."""
+    total = 0.0
+    for cin, cout, k, stride, relu, level in layer_table():
+        h_in, w_in = height >> level, width >> level
+        total += 2.0 * batch * (h_in // stride) * (w_in // stride) * k * k * cin * cout
+    return total
+
+
 def load_params(path=WEIGHTS) -> np.ndarray:
     with np.load(path) as z:
         return z["params"].astype(np.float32)

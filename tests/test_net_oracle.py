@@ -49,3 +49,10 @@ def test_parameter_count():
     from oracle import pm_net_oracle as O
     _, n = O.param_offsets()
     assert 1_500_000 < n < 1_800_000
+
+
+def test_package_layer_table_matches_oracle():
+    from oracle import pm_net_oracle as O
+    from patchmatch_cuda_gb300 import proposal
+    assert proposal.layer_table() == O.layers()
+    assert proposal.forward_flops(192, 320) > 1e9
