@@ -9,7 +9,7 @@ is below the threshold. It is trained here, on the GPU, by the engine's own forw
 backward kernels, on depth maps that plain PatchMatch itself produces on seeded synthetic
 scenes.
 
-    python -m patchmatch_cuda_gb300.proposal train --scenes 2000 --epochs 12 --out weights.npz
+    python -m patchmatch_cuda_gb300.proposal train --scenes 2000 --epochs 30 --out weights.npz
 
 Device memory for inputs and targets comes from torch (plumbing only: no torch operator runs
 on the data path).
@@ -22,6 +22,7 @@ import json
 import multiprocessing as mp
 import os
 import time
+import warnings
 from pathlib import Path
 
 import numpy as np
@@ -129,16 +130,41 @@ def for_engine(engine: Engine, params: np.ndarray | None = None) -> ProposalNet:
     return net
 
 
-def quarter_target(depth: np.ndarray, near: float, far: float, hp: int, wp: int) -> np.ndarray:
-    """Normalised inverse depth (1/d - 1/far) / (1/near - 1/far) of each 4x4 block (mean of
-    1/d), -1 on the padding."""
+def quarter_target_mean(depth: np.ndarray, near: float, far: float, hp: int, wp: int) -> np.ndarray:
+    """Normalised inverse depth (1/d - 1/far) / (1/near - 1/far) of each 4x4 block as the mean
+    of 1/d over all its pixels; -1 on the padding."""
     H, W = depth.shape
     h4, w4 = H // 4, W // 4
     inv = 1.0 / depth[:4 * h4, :4 * w4].astype(np.float64)
     blk = inv.reshape(h4, 4, w4, 4).mean(axis=(1, 3))
-    t = np.clip((blk - 1.0 / far) / (1.0 / near - 1.0 / far), 0.0, 1.0)
     out = np.full((hp, wp), -1.0, np.float32)
-    out[:h4, :w4] = t
+    out[:h4, :w4] = np.clip((blk - 1.0 / far) / (1.0 / near - 1.0 / far), 0.0, 1.0)
+    return out
+
+
+def quarter_target(depth: np.ndarray, near: float, far: float, hp: int, wp: int,
+                   cost: np.ndarray | None = None, max_cost: float = 0.35, min_valid: int = 8) -> np.ndarray:
+    """Normalised inverse depth (1/d - 1/far) / (1/near - 1/far) of each 4x4 block: the median
+    of 1/d over the block's pixels whose best PatchMatch cost (1 - NCC, over the source views)
+    is at most max_cost; -1 (masked) where fewer than min_valid pixels qualify and on the
+    padding. PatchMatch's own costs judge which of its depths to learn from."""
+    H, W = depth.shape
+    h4, w4 = H // 4, W // 4
+    inv = 1.0 / depth[:4 * h4, :4 * w4].astype(np.float64)
+    blocks = inv.reshape(h4, 4, w4, 4).transpose(0, 2, 1, 3).reshape(h4, w4, 16)
+    if cost is not None:
+        ok = cost[:4 * h4, :4 * w4].min(axis=2) <= max_cost
+        ok = ok.reshape(h4, 4, w4, 4).transpose(0, 2, 1, 3).reshape(h4, w4, 16)
+    else:
+        ok = np.ones_like(blocks, bool)
+    vals = np.where(ok, blocks, np.nan)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore", RuntimeWarning)   # blocks without a qualifying pixel
+        med = np.nanmedian(vals, axis=2)
+    t = np.clip((med - 1.0 / far) / (1.0 / near - 1.0 / far), 0.0, 1.0)
+    t[ok.sum(axis=2) < min_valid] = -1.0
+    out = np.full((hp, wp), -1.0, np.float32)
+    out[:h4, :w4] = np.nan_to_num(t, nan=-1.0)
     return out
 
 
@@ -160,9 +186,11 @@ def _make_scene(i: int):
     return i, [(im.K, im.R, im.T, im.image) for im in sv.images], sv.ref_id
 
 
-def make_dataset(n_scenes: int, workers: int = 8, log=print):
+def make_dataset(n_scenes: int, workers: int = 8, target: str = "mean", log=print):
     """Inputs [n, hp, wp, 17] and targets [n, hp, wp] (torch CUDA tensors): the proposal input
-    of each seeded 640x480 scene and its plain-PatchMatch depth map (5 iterations)."""
+    of each seeded 640x480 scene and its plain-PatchMatch depth map (5 iterations), as the mean
+    inverse depth of each 4x4 block ("mean", the committed weights' recipe) or the median over
+    the pixels PatchMatch's own costs deem reliable ("confident")."""
     import torch
     from . import Image
     ctx = mp.get_context("spawn")
@@ -175,12 +203,17 @@ def make_dataset(n_scenes: int, workers: int = 8, log=print):
             eng = Engine(images, ref_id, wl.params())
             eng.run()
             depth = eng.depth()
+            cost = eng.costs()
             hp, wp = eng.proposal_shape()
             if inputs is None:
                 inputs = torch.empty((n_scenes, hp, wp, IN_CH), device="cuda")
                 targets = torch.empty((n_scenes, hp, wp), device="cuda")
             eng.proposal_input(inputs[k].data_ptr())
-            targets[k] = torch.from_numpy(quarter_target(depth, wl.depth_near, wl.depth_far, hp, wp))
+            if target == "mean":
+                tq = quarter_target_mean(depth, wl.depth_near, wl.depth_far, hp, wp)
+            else:
+                tq = quarter_target(depth, wl.depth_near, wl.depth_far, hp, wp, cost)
+            targets[k] = torch.from_numpy(tq)
             eng.close()
             if (k + 1) % 200 == 0:
                 log(f"dataset {k + 1}/{n_scenes} ({time.time() - t0:.0f} s)")
@@ -237,19 +270,20 @@ def main(argv=None):
     sub = ap.add_subparsers(dest="cmd", required=True)
     tr = sub.add_parser("train")
     tr.add_argument("--scenes", type=int, default=2000)
-    tr.add_argument("--epochs", type=int, default=12)
+    tr.add_argument("--epochs", type=int, default=30)
     tr.add_argument("--batch", type=int, default=16)
     tr.add_argument("--lr", type=float, default=5e-4)
     tr.add_argument("--workers", type=int, default=12)
+    tr.add_argument("--target", choices=["mean", "confident"], default="mean")
     tr.add_argument("--out", default=str(WEIGHTS))
     a = ap.parse_args(argv)
     if a.cmd == "train":
         t0 = time.time()
-        x, t = make_dataset(a.scenes, a.workers)
+        x, t = make_dataset(a.scenes, a.workers, a.target)
         t1 = time.time()
         print(f"dataset: {a.scenes} scenes in {t1 - t0:.0f} s", flush=True)
         net, hist = train(x, t, a.epochs, a.batch, a.lr)
-        net.save(a.out, scenes=a.scenes, epochs=a.epochs, batch=a.batch, lr=a.lr, history=hist,
+        net.save(a.out, scenes=a.scenes, epochs=a.epochs, batch=a.batch, lr=a.lr, target=a.target, history=hist,
                  dataset_s=round(t1 - t0, 1), train_s=round(time.time() - t1, 1),
                  workload="seeded 640x480 scenes of 12 planes + 200 boxes, 1 ref + 6 sources, depth [1, 20]")
         print(f"saved {a.out}", flush=True)
