@@ -514,12 +514,14 @@ def run_batched(args):
     import torch
     world, rank, local = dist_setup(True)
     torch.cuda.set_device(local)
-    from patchmatch_cuda_gb300 import Engine, run_batch, scene
+    from patchmatch_cuda_gb300 import Batch, Engine, scene
     refs = scene.make_batch(seed=33 + rank)
     engines = [Engine(sv.images, sv.ref_id, sv.workload.params(gpu_id=local)) for sv in refs]
     stream = torch.cuda.ExternalStream(engines[0].stream())
+    batch = Batch(engines)                       # tunes warps per line, captures the graph
+    info = batch.info()
     for _ in range(max(args.warmup, 1)):
-        run_batch(engines)
+        batch.run()
     evals = sum(e.stats().cost_evals for e in engines)
     barrier(world)
     ms = []
@@ -527,7 +529,7 @@ def run_batched(args):
         for _ in range(args.steps):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            run_batch(engines)
+            batch.run()
             e1.record(stream)
             e1.synchronize()
             ms.append(e0.elapsed_time(e1))
@@ -543,9 +545,13 @@ def run_batched(args):
             "config": {"workload": "batch24_mixed", "references": len(refs),
                        "sizes": sorted({f"{sv.workload.width}x{sv.workload.height}" for sv in refs}),
                        "sources": [sv.workload.n_src for sv in refs], "window": 15, "iterations": 5,
-                       "ms_per_batch": total_ms / args.steps, "mean_bad_pixel_pct_1pct": round(100 * float(np.mean(bad)), 3)},
-            "gpu_launches": None, "clocks": clocks.summary(),
+                       "ms_per_batch": total_ms / args.steps, "mean_bad_pixel_pct_1pct": round(100 * float(np.mean(bad)), 3),
+                       "texels": "u8 (the 8-bit inputs; half the bytes of FP16)",
+                       "schedule": "one CUDA graph per batch; one launch per sweep over all references of a group",
+                       "warps_per_line": info["warps_per_line"]},
+            "gpu_launches": info["launches"] * args.steps, "clocks": clocks.summary(),
         }), flush=True)
+    batch.close()
     for e in engines:
         e.close()
     return 0

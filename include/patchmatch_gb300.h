@@ -166,6 +166,20 @@ pm_status pm_synchronize(pm_handle *h);
  * window size); synchronous. */
 pm_status pm_run_batch(pm_handle *const *hs, int n);
 
+/* A reusable batch (no counterpart in the reference): pm_batch_create groups the handles by
+ * window side and sampler, times 1 .. 6 warps per line on one sweep of each group and
+ * orientation (the autotuner), and captures the whole schedule -- every reference's
+ * initialisation and initial costs, then one launch per sweep over the lines of all references
+ * of a group -- as one CUDA graph on the first handle's stream. pm_batch_run launches the graph
+ * and waits; results and stats are read per handle. The handles must outlive the batch and
+ * their parameters stay as they were at creation. pm_batch_info reports the kernel launches
+ * per run, the number of groups and the tuned warps per line (vertical, horizontal) per group. */
+typedef struct pm_batch pm_batch;
+pm_status pm_batch_create(pm_handle *const *hs, int n, pm_batch **out);
+pm_status pm_batch_run(pm_batch *b);
+pm_status pm_batch_info(const pm_batch *b, int *launches, int *groups, int *wpl, int max_groups);
+pm_status pm_batch_destroy(pm_batch *b);
+
 /* Results. dst_pitch in bytes (0 = width * sizeof(float)). */
 pm_status pm_get_depth(pm_handle *h, float *dst, size_t dst_pitch);
 /* num_samples layers of height*width bytes: layer j, row y, column x holds the view

@@ -26,7 +26,7 @@ from ._native import (DIR_BOTTOM_TO_TOP, DIR_LEFT_TO_RIGHT, DIR_RIGHT_TO_LEFT, D
                       PmView)
 
 __all__ = [
-    "Image", "PatchMatch", "Engine", "read_middlebury", "read_pnm", "write_pgm", "default_params",
+    "Image", "PatchMatch", "Engine", "Batch", "run_batch", "read_middlebury", "read_pnm", "write_pgm", "default_params",
     "load_depth_file", "PatchMatchError", "PREFILTER_NONE", "PREFILTER_BOX", "PREFILTER_GAUSSIAN",
     "PRECISION_FP32", "PRECISION_MIXED", "DIR_LEFT_TO_RIGHT", "DIR_TOP_TO_BOTTOM",
     "DIR_RIGHT_TO_LEFT", "DIR_BOTTOM_TO_TOP", "INIT_RANDOM", "INIT_PROPOSAL",
@@ -285,6 +285,39 @@ def run_batch(engines: Sequence[Engine]) -> None:
     lib = _native.load_engine()
     arr = (C.c_void_p * len(engines))(*[e.h for e in engines])
     _native.check(lib.pm_run_batch(arr, len(engines)))
+
+
+class Batch:
+    """A reusable batch of engines (pm_batch): tuned warps per line, schedule captured as one
+    CUDA graph. The engines must stay open while the batch lives."""
+
+    def __init__(self, engines: Sequence[Engine]):
+        self._lib = _native.load_engine()
+        self.engines = list(engines)
+        arr = (C.c_void_p * len(self.engines))(*[e.h for e in self.engines])
+        self.h = C.c_void_p()
+        _native.check(self._lib.pm_batch_create(arr, len(self.engines), C.byref(self.h)))
+
+    def run(self) -> None:
+        _native.check(self._lib.pm_batch_run(self.h))
+
+    def info(self) -> dict:
+        launches, groups = C.c_int(), C.c_int()
+        wpl = (C.c_int * 128)()
+        _native.check(self._lib.pm_batch_info(self.h, C.byref(launches), C.byref(groups), wpl, 64))
+        return {"launches": launches.value, "groups": groups.value,
+                "warps_per_line": [(wpl[2 * i], wpl[2 * i + 1]) for i in range(groups.value)]}
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self._lib.pm_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class PatchMatch:

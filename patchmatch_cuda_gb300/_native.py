@@ -37,7 +37,8 @@ EXPORTED_SYMBOLS = [
     "pm_transpose_layers", "pm_philox", "pm_box_moments_noalloc", "pm_check_reciprocal",
     "pm_gemm_bf16", "pm_gemm_error", "pm_net_create", "pm_net_destroy", "pm_net_num_params",
     "pm_net_get_params", "pm_net_set_params", "pm_net_forward", "pm_net_gradients", "pm_net_train_step",
-    "pm_net_layout", "pm_net_size", "pm_set_proposal", "pm_proposal_input",
+    "pm_net_layout", "pm_net_size", "pm_set_proposal", "pm_proposal_input", "pm_batch_create",
+    "pm_batch_run", "pm_batch_info", "pm_batch_destroy",
 ]
 
 
@@ -132,6 +133,10 @@ def load_engine() -> C.CDLL:
         "pm_net_size": (C.c_int, [P, P, P, P]),
         "pm_set_proposal": (C.c_int, [H, P]),
         "pm_proposal_input": (C.c_int, [H, P, P, P]),
+        "pm_batch_create": (C.c_int, [P, C.c_int, P]),
+        "pm_batch_run": (C.c_int, [P]),
+        "pm_batch_info": (C.c_int, [P, P, P, P, C.c_int]),
+        "pm_batch_destroy": (C.c_int, [P]),
         "pm_box_moments_noalloc": (C.c_int, [P, C.c_size_t, C.c_int, C.c_int, C.c_int, P, P, P, C.c_size_t, P]),
     }
     for name, (res, args) in sig.items():

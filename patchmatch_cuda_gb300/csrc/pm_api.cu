@@ -872,19 +872,137 @@ pm_status pm_run(pm_handle *h)
     return PM_OK;
 }
 
-pm_status pm_run_batch(pm_handle *const *hs, int n)
+}  // extern "C"
+
+// A batch of references on one device: groups of equal window side and sampler, each with a
+// device array of descriptors; every sweep of a group is one launch over the lines of all of
+// its references.
+struct pm_batch {
+    struct Group {
+        std::vector<pm_handle *> refs;
+        RefDesc *d_descs = nullptr;
+        int win = 0;
+        bool hw = false;
+        int wpl[2] = {0, 0};  // warps per line: vertical, horizontal sweeps (0: occupancy rule)
+    };
+    std::vector<pm_handle *> hs;
+    std::vector<Group> groups;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    int launches = 0;
+};
+
+namespace {
+
+// Initialisation, initial costs and every sweep of the batch on stream s.
+cudaError_t enqueue_batch(pm_batch *b, cudaStream_t s)
+{
+    b->launches = 0;
+    for (pm_batch::Group &g : b->groups) {
+        const int m = (int)g.refs.size();
+        int max_sweeps = 0;
+        for (int i = 0; i < m; ++i) {
+            pm_handle *h = g.refs[i];
+            cudaError_t e = cudaMemsetAsync(h->d_evals, 0, 2 * sizeof(unsigned long long), s);
+            if (e == cudaSuccess)
+                e = h->p.init_mode == PM_INIT_PROPOSAL ? enqueue_proposal_init(h, s)
+                                                      : launch_init_depth(g.d_descs, i, h->W * h->H, s);
+            if (e != cudaSuccess) return e;
+            LaunchReq req{};
+            req.kind = LaunchKind::Costs;
+            req.stream = s;
+            req.refs = g.d_descs;
+            req.ref_index = i;
+            req.axis = 1;
+            req.grid = (h->W * h->H + COST_BLOCK / 32 - 1) / (COST_BLOCK / 32);
+            e = launch_window(h->win, hw_of(h), req);
+            if (e != cudaSuccess) return e;
+            b->launches += 2;
+            max_sweeps = std::max(max_sweeps, schedule_sweeps(h));
+        }
+        for (int k = 0; k < max_sweeps; ++k) {
+            const int it = k / 4, d = k % 4;
+            // references still sweeping at k, in descriptor order
+            std::vector<int> lines(m, 0);
+            for (int i = 0; i < m; ++i) lines[i] = schedule_sweeps(g.refs[i]) > k ? lines_of(g.refs[i], d) : 0;
+            SweepArgs a;
+            // one view sample in the first iteration after a random initialisation
+            // (patchMatch.cu:307-316); a group mixing both initialisations follows its first
+            // reference. Every sweep records the sampled views; a reference's last writes last.
+            const int s_first = g.refs[0]->p.init_mode == PM_INIT_RANDOM ? 1 : 0;
+            fill_sweep_args(a, g.d_descs, lines.data(), m, d, (uint32_t)k, it == 0 ? s_first : 0, 1);
+            a.perturb = sweep_perturb(g.refs[0], k);
+            const int wpl = g.wpl[orient(d)] ? g.wpl[orient(d)] : batch_wpl(g.win, g.hw, a.total_lines, b->hs[0]->device);
+            const cudaError_t e = enqueue_sweep(g.win, g.hw, wpl, a, s);
+            if (e != cudaSuccess) return e;
+            ++b->launches;
+        }
+    }
+    return cudaGetLastError();
+}
+
+// Warps per line for each group and orientation: the fastest of 1 .. MAX_WARPS_PER_LINE on one
+// sweep of the whole group (after its initialisation and initial costs).
+cudaError_t tune_batch(pm_batch *b, cudaEvent_t e0, cudaEvent_t e1)
+{
+    cudaStream_t s = b->stream;
+    for (pm_batch::Group &g : b->groups) {
+        // a state to sweep: random initialisation and initial costs of every reference
+        cudaError_t e = cudaSuccess;
+        const int m = (int)g.refs.size();
+        for (int i = 0; i < m && e == cudaSuccess; ++i) {
+            pm_handle *h = g.refs[i];
+            e = launch_init_depth(g.d_descs, i, h->W * h->H, s);
+            LaunchReq req{};
+            req.kind = LaunchKind::Costs;
+            req.stream = s;
+            req.refs = g.d_descs;
+            req.ref_index = i;
+            req.axis = 1;
+            req.grid = (h->W * h->H + COST_BLOCK / 32 - 1) / (COST_BLOCK / 32);
+            if (e == cudaSuccess) e = launch_window(h->win, hw_of(h), req);
+        }
+        if (e != cudaSuccess) return e;
+        for (int o = 0; o < 2; ++o) {
+            const int d = o == 0 ? PM_DIR_TOP_TO_BOTTOM : PM_DIR_LEFT_TO_RIGHT;
+            std::vector<int> lines;
+            for (pm_handle *h : g.refs) lines.push_back(lines_of(h, d));
+            float best_ms = 1e30f;
+            for (int wpl = 1; wpl <= MAX_WARPS_PER_LINE; ++wpl) {
+                SweepArgs a;
+                fill_sweep_args(a, g.d_descs, lines.data(), m, d, 0xFFFFFFF0u, 0, 0);
+                float ms = 0.0f;
+                for (int rep = 0; rep < 2; ++rep) {  // the first launch warms the caches
+                    e = cudaEventRecord(e0, s);
+                    if (e == cudaSuccess) e = enqueue_sweep(g.win, g.hw, wpl, a, s);
+                    if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+                    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+                    if (e != cudaSuccess) return e;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                }
+                if (ms < best_ms) {
+                    best_ms = ms;
+                    g.wpl[o] = wpl;
+                }
+            }
+        }
+    }
+    return cudaSuccess;
+}
+
+pm_status batch_setup(pm_handle *const *hs, int n, pm_batch *b)
 {
     if (!hs || n < 1) return PM_ERR_INVALID_ARGUMENT;
     for (int i = 0; i < n; ++i) {
         if (!hs[i]) return PM_ERR_INVALID_ARGUMENT;
         if (hs[i]->device != hs[0]->device) return PM_ERR_UNSUPPORTED;
+        if (hs[i]->p.init_mode == PM_INIT_PROPOSAL && !hs[i]->net) return PM_ERR_STATE;
     }
-    pm_handle *h0 = hs[0];
-    pm_status st = set_device(h0);
+    pm_status st = set_device(hs[0]);
     if (st != PM_OK) return st;
     for (int i = 0; i < n; ++i) PM_CUDA(hs[i], cudaStreamSynchronize(hs[i]->stream));
-    cudaStream_t s = h0->stream;
-    // group by window side and sampler; each group sweeps in one launch per direction
+    b->hs.assign(hs, hs + n);
+    b->stream = hs[0]->stream;
     std::vector<int> done(n, 0);
     for (int g0 = 0; g0 < n; ++g0) {
         if (done[g0]) continue;
@@ -895,55 +1013,113 @@ pm_status pm_run_batch(pm_handle *const *hs, int n)
                 done[i] = 1;
             }
         for (size_t start = 0; start < grp.size(); start += MAX_BATCH_REFS) {
-            const int m = (int)std::min<size_t>(MAX_BATCH_REFS, grp.size() - start);
-            RefDesc *d_descs = nullptr;
-            PM_CUDA(h0, cudaMallocAsync((void **)&d_descs, sizeof(RefDesc) * m, s));
-            int max_sweeps = 0;
-            for (int i = 0; i < m; ++i) {
-                pm_handle *h = grp[start + i];
-                PM_CUDA(h0, cudaMemcpyAsync(d_descs + i, &h->h_desc, sizeof(RefDesc),
-                                            cudaMemcpyHostToDevice, s));
-                PM_CUDA(h0, cudaMemsetAsync(h->d_evals, 0, 2 * sizeof(unsigned long long), s));
-                if (h->p.init_mode == PM_INIT_PROPOSAL) PM_CUDA(h0, enqueue_proposal_init(h, s));
-                else PM_CUDA(h0, launch_init_depth(d_descs, i, h->W * h->H, s));
-                LaunchReq req{};
-                req.kind = LaunchKind::Costs;
-                req.stream = s;
-                req.refs = d_descs;
-                req.ref_index = i;
-                req.axis = 1;
-                req.grid = (h->W * h->H + COST_BLOCK / 32 - 1) / (COST_BLOCK / 32);
-                PM_CUDA(h0, launch_window(h->win, hw_of(h), req));
-                max_sweeps = std::max(max_sweeps, schedule_sweeps(h));
-            }
-            std::vector<SweepArgs> args((size_t)max_sweeps);
-            for (int k = 0; k < max_sweeps; ++k) {
-                const int it = k / 4, d = k % 4;
-                // references still sweeping at k, in descriptor order
-                std::vector<int> lines(m, 0);
-                for (int i = 0; i < m; ++i)
-                    lines[i] = schedule_sweeps(grp[start + i]) > k ? lines_of(grp[start + i], d) : 0;
-                // every sweep records the sampled views; a reference's last one writes last
-                SweepArgs &a = args[(size_t)k];
-                // one view sample in the first iteration after a random initialisation
-                // (patchMatch.cu:307-316); a batch mixing both initialisations follows the first
-                const int s_first = grp[start]->p.init_mode == PM_INIT_RANDOM ? 1 : 0;
-                fill_sweep_args(a, d_descs, lines.data(), m, d, (uint32_t)k, it == 0 ? s_first : 0, 1);
-                a.perturb = sweep_perturb(grp[start], k);
-                PM_CUDA(h0, enqueue_sweep(grp[start]->win, hw_of(grp[start]),
-                                          batch_wpl(grp[start]->win, hw_of(grp[start]), a.total_lines, h0->device), a, s));
-            }
-            PM_CUDA(h0, cudaFreeAsync(d_descs, s));
+            pm_batch::Group g;
+            g.refs.assign(grp.begin() + start, grp.begin() + std::min(grp.size(), start + MAX_BATCH_REFS));
+            g.win = grp[0]->win;
+            g.hw = hw_of(grp[0]);
+            PM_CUDA(hs[0], cudaMalloc((void **)&g.d_descs, sizeof(RefDesc) * g.refs.size()));
+            for (size_t i = 0; i < g.refs.size(); ++i)
+                PM_CUDA(hs[0], cudaMemcpy(g.d_descs + i, &g.refs[i]->h_desc, sizeof(RefDesc), cudaMemcpyHostToDevice));
+            b->groups.push_back(g);
         }
     }
-    PM_CUDA(h0, cudaStreamSynchronize(s));
-    for (int i = 0; i < n; ++i) {
+    return PM_OK;
+}
+
+void batch_free(pm_batch *b)
+{
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    for (pm_batch::Group &g : b->groups)
+        if (g.d_descs) cudaFree(g.d_descs);
+}
+
+pm_status batch_finish(pm_batch *b)
+{
+    PM_CUDA(b->hs[0], cudaStreamSynchronize(b->stream));
+    for (pm_handle *h : b->hs) {
         unsigned long long ev[2];
-        PM_CUDA(hs[i], cudaMemcpy(ev, hs[i]->d_evals, sizeof ev, cudaMemcpyDeviceToHost));
-        hs[i]->stats.cost_evals = ev[0];
-        hs[i]->stats.cost_evals_done = ev[1];
-        hs[i]->ran = true;
+        PM_CUDA(h, cudaMemcpy(ev, h->d_evals, sizeof ev, cudaMemcpyDeviceToHost));
+        h->stats.cost_evals = ev[0];
+        h->stats.cost_evals_done = ev[1];
+        h->ran = true;
     }
+    return PM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+pm_status pm_run_batch(pm_handle *const *hs, int n)
+{
+    pm_batch b;
+    pm_status st = batch_setup(hs, n, &b);
+    if (st == PM_OK) {
+        const cudaError_t e = enqueue_batch(&b, b.stream);
+        st = e == cudaSuccess ? batch_finish(&b) : cuda_fail(hs[0], e, "batch schedule");
+    }
+    batch_free(&b);
+    return st;
+}
+
+pm_status pm_batch_create(pm_handle *const *hs, int n, pm_batch **out)
+{
+    if (!out) return PM_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    pm_batch *b = new pm_batch();
+    pm_status st = batch_setup(hs, n, b);
+    if (st == PM_OK) {
+        pm_handle *h0 = hs[0];
+        cudaError_t e = tune_batch(b, h0->ev[2], h0->ev[3]);
+        cudaGraph_t g = nullptr;
+        if (e == cudaSuccess) e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            const cudaError_t e1 = enqueue_batch(b, b->stream);
+            const cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
+            e = e1 != cudaSuccess ? e1 : e2;
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&b->graph, g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (e != cudaSuccess) st = cuda_fail(h0, e, "batch graph");
+    }
+    if (st != PM_OK) {
+        batch_free(b);
+        delete b;
+        return st;
+    }
+    *out = b;
+    return PM_OK;
+}
+
+pm_status pm_batch_run(pm_batch *b)
+{
+    if (!b) return PM_ERR_INVALID_ARGUMENT;
+    pm_status st = set_device(b->hs[0]);
+    if (st != PM_OK) return st;
+    PM_CUDA(b->hs[0], cudaGraphLaunch(b->graph, b->stream));
+    return batch_finish(b);
+}
+
+pm_status pm_batch_info(const pm_batch *b, int *launches, int *groups, int *wpl, int max_groups)
+{
+    if (!b) return PM_ERR_INVALID_ARGUMENT;
+    if (launches) *launches = b->launches;
+    if (groups) *groups = (int)b->groups.size();
+    if (wpl)
+        for (int i = 0; i < (int)b->groups.size() && i < max_groups; ++i) {
+            wpl[2 * i] = b->groups[i].wpl[0];
+            wpl[2 * i + 1] = b->groups[i].wpl[1];
+        }
+    return PM_OK;
+}
+
+pm_status pm_batch_destroy(pm_batch *b)
+{
+    if (!b) return PM_OK;
+    set_device(b->hs[0]);
+    cudaStreamSynchronize(b->stream);
+    batch_free(b);
+    delete b;
     return PM_OK;
 }
 

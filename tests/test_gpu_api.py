@@ -164,3 +164,29 @@ def test_ground_truth_accuracy_small_scene(parity_log):
     parity_log("gt_plane3_320x240", bad1=bad1, bad5=bad5)
     assert bad1 < 0.15 and bad5 < 0.05
     eng.close()
+
+
+def test_graph_batch_equals_single_runs(small):
+    """pm_batch: tuned warps per line and one CUDA graph for the whole schedule; two launches of
+    the graph reproduce the single runs exactly."""
+    from patchmatch_cuda_gb300 import Batch, scene
+    w2 = scene.Workload("api_g", 160, 120, 4, 4, 3, 2.0, 8.0, 3, 0, seed=23)
+    sv2 = scene.make_views(w2)
+    singles = []
+    for sv in (small, sv2):
+        e = _engine(sv)
+        e.run()
+        singles.append(e.depth())
+        e.close()
+    engines = [_engine(small), _engine(sv2)]
+    b = Batch(engines)
+    info = b.info()
+    assert info["groups"] >= 1 and info["launches"] > 0
+    assert all(1 <= v <= 6 for pair in info["warps_per_line"] for v in pair)
+    for _ in range(2):
+        b.run()
+        for e, d in zip(engines, singles):
+            np.testing.assert_array_equal(e.depth(), d)
+    b.close()
+    for e in engines:
+        e.close()
