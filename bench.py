@@ -48,6 +48,8 @@ def parse_args():
     ap.add_argument("--profile", type=int, default=None, metavar="DIR",
                     help="run only the initial state and one sweep in direction DIR (for ncu)")
     ap.add_argument("--threads-per-line", type=int, default=0)
+    ap.add_argument("--learned", type=int, default=0, metavar="SWEEPS",
+                    help="batched workloads: learned initialisation followed by SWEEPS sweeps")
     ap.add_argument("--profile-net", action="store_true",
                     help="run only the proposal network's forward pass on the workload (for ncu)")
     return ap.parse_args()
@@ -514,9 +516,22 @@ def run_batched(args):
     import torch
     world, rank, local = dist_setup(True)
     torch.cuda.set_device(local)
-    from patchmatch_cuda_gb300 import Batch, Engine, scene
-    refs = scene.make_batch(seed=33 + rank)
-    engines = [Engine(sv.images, sv.ref_id, sv.workload.params(gpu_id=local)) for sv in refs]
+    from patchmatch_cuda_gb300 import INIT_PROPOSAL, Batch, Engine, proposal, scene
+    full = args.workload == "full8_3072x2048"
+    refs = scene.make_full_batch() if full else scene.make_batch(seed=33 + rank)
+    over = {}
+    if args.learned:
+        over = dict(init_mode=INIT_PROPOSAL, num_sweeps=args.learned, perturbation=0.05)
+    engines = [Engine(sv.images, sv.ref_id, sv.workload.params(gpu_id=local, **over)) for sv in refs]
+    nets = {}
+    if args.learned:   # one network per reference size, shared (the batch runs them in turn)
+        params = proposal.load_params()
+        for e in engines:
+            shape = e.proposal_shape()
+            if shape not in nets:
+                nets[shape] = proposal.ProposalNet(1, *shape)
+                nets[shape].set_params(params)
+            e.set_proposal(nets[shape])
     stream = torch.cuda.ExternalStream(engines[0].stream())
     batch = Batch(engines)                       # tunes warps per line, captures the graph
     info = batch.info()
@@ -541,10 +556,12 @@ def run_batched(args):
             "metric": "G cost-evals/s", "value": total_evals / (total_ms * 1e-3) / 1e9, "unit": "G cost-evals/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8 texels, f32 arithmetic",
-            "data": "synthetic (one scene of 40 planes + 500 boxes)",
-            "config": {"workload": "batch24_mixed", "references": len(refs),
+            "data": "synthetic (one scene of 60 planes + 2000 boxes)" if full else "synthetic (one scene of 40 planes + 500 boxes)",
+            "config": {"workload": args.workload, "references": len(refs),
+                       "init": f"learned proposal + {args.learned} sweeps" if args.learned else "random (plain PatchMatch)",
                        "sizes": sorted({f"{sv.workload.width}x{sv.workload.height}" for sv in refs}),
-                       "sources": [sv.workload.n_src for sv in refs], "window": 15, "iterations": 5,
+                       "sources": [sv.workload.n_src for sv in refs], "window": 2 * refs[0].workload.half_window + 1,
+                       "iterations": refs[0].workload.iterations,
                        "ms_per_batch": total_ms / args.steps, "mean_bad_pixel_pct_1pct": round(100 * float(np.mean(bad)), 3),
                        "texels": "u8 (the 8-bit inputs; half the bytes of FP16)",
                        "schedule": "one CUDA graph per batch; one launch per sweep over all references of a group",
@@ -554,12 +571,14 @@ def run_batched(args):
     batch.close()
     for e in engines:
         e.close()
+    for n in nets.values():
+        n.close()
     return 0
 
 
 def main():
     args = parse_args()
-    if args.workload == "batch24_mixed" and args.impl == "ours":
+    if args.workload in ("batch24_mixed", "full8_3072x2048") and args.impl == "ours":
         import numpy as np  # noqa: F401
         return run_batched(args)
     if args.profile is not None:

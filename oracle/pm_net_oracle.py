@@ -4,8 +4,8 @@ A float64 numpy restatement of the encoder-decoder that patchmatch_cuda_gb300/cs
 trains on the GPU: the same layers, the same parameter layout (per layer: weights
 [cout][ky][kx][cin], then the bias), the same loss (L1 of the relative inverse-depth error,
 the inverse depth read from the sigmoid of output 0, plus 0.1 x binary cross-entropy of the
-sigmoid of output 1 against "predicted depth within 2 % of the target's"), and its gradients by hand-written backward
-passes. With bf16=True it rounds to bfloat16 exactly where the GPU stores bfloat16 (the
+sigmoid of output 1 against "predicted depth within 2 % of the target's"), and its gradients
+by hand-written backward passes. With bf16=True it rounds to bfloat16 exactly where the GPU stores bfloat16 (the
 input, the weights, every activation and the convolution output gradients), so the remaining
 difference is the order of FP32 accumulation. The reference project has no learned part:
 this oracle checks the engine's own kernels, and the tests only use it as the checker.
@@ -141,7 +141,6 @@ def forward_backward(params, x, target, inv_far, inv_range, use_bf16=True):
     stats = (float(l1[valid].sum() / max(cnt, 1)), float(bce[valid].sum() / max(cnt, 1)), cnt)
 
     grad = np.zeros(n)
-    gmap = {}
     # backward through the layers in reverse, with the same routing of gradients as the GPU
     g_head = go.reshape(B, H, W, 2)
 

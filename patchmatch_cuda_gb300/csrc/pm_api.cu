@@ -33,7 +33,6 @@ struct pm_handle {
     uint8_t *d_view_sel = nullptr;
     unsigned long long *d_evals = nullptr;
     float4 *d_hh = nullptr;
-    double *d_hh64 = nullptr;
     RefDesc *d_desc = nullptr;
     RefDesc h_desc{};
     cudaArray_t arr[MAX_VIEWS] = {};
@@ -475,7 +474,7 @@ pm_status pm_destroy(pm_handle *h)
     if (h->tex_layered) cudaDestroyTextureObject(h->tex_layered);
     if (h->layered) release_array(h->device, h->layer_w, h->layer_h, h->texel_bytes, h->layered, h->V);
     void *bufs[] = {h->d_ref, h->d_sum_i, h->d_sum_ii, h->d_c1, h->d_depth, h->d_cost, h->d_beta,
-                    h->d_view_sel, h->d_evals, h->d_hh, h->d_hh64, h->d_desc, h->d_quarter[0],
+                    h->d_view_sel, h->d_evals, h->d_hh, h->d_desc, h->d_quarter[0],
                     h->d_quarter[1], h->d_quarter[2], h->d_prop_in, h->d_prop_out};
     for (void *b : bufs)
         if (b) cudaFreeAsync(b, h->stream);
@@ -552,7 +551,6 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
     for (int i = 0; i < 9; ++i) kr[i] = ref.K[i];
     if (!inv3(kr, kr_inv)) { pm_destroy(h); return PM_ERR_CAMERA; }
     std::vector<float> hh((size_t)h->V * 20, 0.0f);
-    std::vector<double> hh64((size_t)h->V * 18);
     int si = 0;
     for (int i = 0; i < n_views; ++i) {
         if (i == ref_id) continue;
@@ -561,7 +559,6 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
         for (int k = 0; k < 18; ++k) {
             if (!std::isfinite(o[k])) { pm_destroy(h); return PM_ERR_CAMERA; }
             hh[(size_t)si * 20 + k] = (float)o[k];
-            hh64[(size_t)si * 18 + k] = o[k];
         }
         h->src_w[si] = views[i].width;
         h->src_h[si] = views[i].height;
@@ -641,7 +638,6 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
     PM_TRY(dalloc(&h->d_view_sel, npix * (size_t)p.num_samples, s));
     PM_TRY(dalloc(&h->d_evals, 2 * sizeof(unsigned long long), s));
     PM_TRY(dalloc(&h->d_hh, hh.size() * 4, s));
-    PM_TRY(dalloc(&h->d_hh64, hh64.size() * 8, s));
     PM_TRY(dalloc(&h->d_desc, sizeof(RefDesc), s));
     if (h->geom.w4 > 0 && h->geom.h4 > 0) {
         PM_TRY(dalloc(&h->d_quarter[0], (size_t)h->geom.w4 * h->geom.h4 * 4 + 16, s));
@@ -651,7 +647,6 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
     PM_TRY(cudaMemsetAsync(h->d_view_sel, 255, npix * (size_t)p.num_samples, s));
     PM_TRY(cudaMemsetAsync(h->d_evals, 0, 2 * sizeof(unsigned long long), s));
     PM_TRY(cudaMemcpyAsync(h->d_hh, hh.data(), hh.size() * 4, cudaMemcpyHostToDevice, s));
-    PM_TRY(cudaMemcpyAsync(h->d_hh64, hh64.data(), hh64.size() * 8, cudaMemcpyHostToDevice, s));
 
     // images: u8 upload -> float texels (-> prefilter) -> reference maps / source arrays
     int max_w = 0, max_h = 0;
@@ -804,7 +799,6 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
     D.view_sel = h->d_view_sel;
     D.evals = h->d_evals;
     D.hh = h->d_hh;
-    D.hh64 = h->d_hh64;
     D.tex_layered = h->tex_layered;
     for (int v = 0; v < h->V; ++v) {
         D.tex[v] = h->tex[v];
@@ -1077,6 +1071,20 @@ pm_status pm_batch_create(pm_handle *const *hs, int n, pm_batch **out)
             const cudaError_t e1 = enqueue_batch(b, b->stream);
             const cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
             e = e1 != cudaSuccess ? e1 : e2;
+        }
+        if (e == cudaSuccess) {
+            // kernel launches per run: the graph's kernel nodes (the proposal network's
+            // included)
+            size_t n_nodes = 0;
+            e = cudaGraphGetNodes(g, nullptr, &n_nodes);
+            std::vector<cudaGraphNode_t> nodes(n_nodes);
+            if (e == cudaSuccess && n_nodes) e = cudaGraphGetNodes(g, nodes.data(), &n_nodes);
+            int kernels = 0;
+            for (size_t i = 0; e == cudaSuccess && i < n_nodes; ++i) {
+                cudaGraphNodeType t;
+                if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++kernels;
+            }
+            b->launches = kernels;
         }
         if (e == cudaSuccess) e = cudaGraphInstantiate(&b->graph, g, 0);
         if (g) cudaGraphDestroy(g);

@@ -52,7 +52,6 @@ struct RefDesc {
     uint8_t *view_sel;              // num_samples*height*width or null
     unsigned long long *evals;      // [0] algorithmic count, [1] computed count
     const float4 *hh;               // n_src * 5 float4: H1 (9), H2 (9), pad (2)
-    const double *hh64;             // n_src * 18 (mixed precision window origin)
     cudaTextureObject_t tex_layered;  // all sources as layers (texture-filtering sampler)
     cudaTextureObject_t tex[MAX_VIEWS];
     float src_w[MAX_VIEWS], src_h[MAX_VIEWS];

@@ -142,11 +142,7 @@ __global__ void relu_back_kernel(const float *__restrict__ g, int gcs, int gco, 
     const bf16 b = __float2bfloat16(v);
     dz[(size_t)p * N64 + c] = b;
     if (c < 128) dzt[(size_t)c * Ppad + p] = c < N ? b : __float2bfloat16(0.0f);
-    if (dbias && c < N && p < P) {
-        // warp-level pre-sum of identical channels is not possible (lanes differ in c); the
-        // per-thread atomic is cheap next to the GEMMs
-        atomicAdd(dbias + c, v);
-    }
+    if (dbias && c < N && p < P) atomicAdd(dbias + c, v);
 }
 
 // out[c][r] = in[r][c] for a rows x cols BF16 matrix (32 x 32 tiles through shared memory).
@@ -557,8 +553,8 @@ cudaError_t loss(Net &n, const float *target, float inv_far, float inv_range)
 {
     const int P0 = n.B * n.H * n.W;
     cudaMemsetAsync(n.acc, 0, 4 * sizeof(float), n.stream);
-    // the loss is a mean over valid pixels; its scale is applied after counting, so the
-    // gradient is formed with 1/P0 and rescaled by Adam's invariance to a constant factor
+    // the gradient is that of (sum over valid pixels) / P0; Adam's steps do not depend on a
+    // constant factor, and pm_net_gradients reports the loss terms as means over valid pixels
     loss_kernel<<<blocks(P0), 256, 0, n.stream>>>(n.out, HEAD_N, target, P0, inv_far, inv_range, 0.02f, 0.1f,
                                                    1.0f / (float)P0, n.gout_head, HEAD_N, n.acc);
     return cudaGetLastError();

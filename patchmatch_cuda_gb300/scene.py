@@ -10,6 +10,7 @@ index, the reference's ground-truth z-depth and the engine parameters.
     batch24_mixed      24 references of 640x480 / 1280x720 / 1920x1080 with 6-12 sources each
                        from one scene of 40 planes + 500 boxes, 15x15 window, 5 iterations
     box2000_3072x2048  60 planes + 2000 boxes, 1 ref + 20 sources, depth [0.5, 50], 19x19 window
+    full8_3072x2048    8 such references from one scene (make_full_batch), batched
 
 Parameters the workloads leave open are fixed once: numOfSamples 3 for up to 4 sources else 5,
 SPMAlpha 0.45, plane normal (0, 0, 1).
@@ -170,6 +171,32 @@ def make_batch(n_refs: int = 24, seed: int = 33, half_window: int = 7, iteration
         images, gt = [], None
         for i, yaw in enumerate(yaws):
             im, d = sc.view(yaw, pitch, w_, h_, f)
+            images.append(im)
+            if i == ref_id:
+                gt = d
+        out.append(SceneViews(images, ref_id, gt, wl))
+    sc.close()
+    return out
+
+
+def make_full_batch(n_refs: int = 8, seed: int = 55, width: int = 3072, height: int = 2048, n_src: int = 20,
+                    half_window: int = 9, iterations: int = 5, depth_near: float = 0.5,
+                    depth_far: float = 50.0, n_planes: int = 60, n_boxes: int = 2000) -> list[SceneViews]:
+    """The full-scale workload: references of 3072x2048 with 20 sources each (19x19 window,
+    depth [0.5, 50]) from one scene of 60 planes + 2000 boxes, their arcs centred on yaws
+    spread over 30 degrees."""
+    f = 300.0 * width / 320.0
+    sc = Scene(seed, n_planes, n_boxes, depth_near, depth_far, width, height, f)
+    out = []
+    for r in range(n_refs):
+        yaw_c = -15.0 + 30.0 * r / max(1, n_refs - 1)
+        wl = Workload(f"full{r}", width, height, n_src, half_window, iterations, depth_near, depth_far,
+                      n_planes, n_boxes, prefilter=PREFILTER_NONE, seed=seed * 1000 + r)
+        yaws = arc_yaws(n_src + 1, yaw_c)
+        ref_id = n_src // 2
+        images, gt = [], None
+        for i, yaw in enumerate(yaws):
+            im, d = sc.view(yaw, 0.0, width, height, f)
             images.append(im)
             if i == ref_id:
                 gt = d
