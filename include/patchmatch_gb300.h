@@ -260,6 +260,13 @@ pm_status pm_philox(uint64_t seed, int n, const uint32_t *counters, uint32_t *ou
  * reciprocal differs from the correctly rounded one (expected: 0). */
 pm_status pm_check_reciprocal(int exp_shift, unsigned long long *mismatches);
 
+/* ---- texture-filtering peak ----------------------------------------------------------------
+ * No counterpart in the reference: the measured rate (bilinear samples per second) of layered
+ * u8 texture fetches in the NCC's access pattern on the current device, with enough warps to
+ * saturate the texture units -- the roofline the sweep kernel's sample rate is reported
+ * against. Allocates a small texture, runs about 2 ms. */
+pm_status pm_texture_peak(double *samples_per_s);
+
 /* ---- learned proposal on a handle -------------------------------------------------------
  * No counterpart in the reference. pm_set_proposal attaches a network (not owned; NULL
  * detaches) whose batch is 1 and whose size is the handle's proposal size (pm_proposal_input

@@ -38,7 +38,7 @@ EXPORTED_SYMBOLS = [
     "pm_gemm_bf16", "pm_gemm_error", "pm_net_create", "pm_net_destroy", "pm_net_num_params",
     "pm_net_get_params", "pm_net_set_params", "pm_net_forward", "pm_net_gradients", "pm_net_train_step",
     "pm_net_layout", "pm_net_size", "pm_set_proposal", "pm_proposal_input", "pm_batch_create",
-    "pm_batch_run", "pm_batch_info", "pm_batch_destroy",
+    "pm_batch_run", "pm_batch_info", "pm_batch_destroy", "pm_texture_peak",
 ]
 
 
@@ -137,6 +137,7 @@ def load_engine() -> C.CDLL:
         "pm_batch_run": (C.c_int, [P]),
         "pm_batch_info": (C.c_int, [P, P, P, P, C.c_int]),
         "pm_batch_destroy": (C.c_int, [P]),
+        "pm_texture_peak": (C.c_int, [P]),
         "pm_box_moments_noalloc": (C.c_int, [P, C.c_size_t, C.c_int, C.c_int, C.c_int, P, P, P, C.c_size_t, P]),
     }
     for name, (res, args) in sig.items():

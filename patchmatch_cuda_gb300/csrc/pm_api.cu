@@ -1457,6 +1457,17 @@ pm_status pm_philox(uint64_t seed, int n, const uint32_t *counters, uint32_t *ou
     return PM_OK;
 }
 
+pm_status pm_texture_peak(double *samples_per_s)
+{
+    if (!samples_per_s) return PM_ERR_INVALID_ARGUMENT;
+    const cudaError_t e = measure_texture_peak(samples_per_s);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return PM_ERR_CUDA;
+    }
+    return PM_OK;
+}
+
 pm_status pm_check_reciprocal(int exp_shift, unsigned long long *mismatches)
 {
     if (!mismatches || exp_shift < -120 || exp_shift > 120) return PM_ERR_INVALID_ARGUMENT;

@@ -70,6 +70,7 @@ cudaError_t launch_transpose(const float *in, size_t in_pitch, float *out, size_
 cudaError_t launch_philox(uint64_t seed, int n, const uint32_t *ctr, uint32_t *out,
                           cudaStream_t s);
 cudaError_t launch_check_rcp(int exp_shift, unsigned long long *mismatches, cudaStream_t s);
+cudaError_t measure_texture_peak(double *samples_per_s);
 
 // Learned proposal (pm_proposal.cu): quarter-resolution images, the plane-sweep input of the
 // network (17 channels), and the initial depth from its output.

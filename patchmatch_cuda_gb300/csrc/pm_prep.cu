@@ -227,4 +227,71 @@ cudaError_t launch_check_rcp(int exp_shift, unsigned long long *mismatches, cuda
     return cudaGetLastError();
 }
 
+
+// Texture-filtering throughput of a layered u8 texture in the NCC's access pattern (half-warps
+// of 16 adjacent columns, 15 rows per loop, coordinates kept inside the texture): the peak the
+// sweep kernel's sample rate is compared with.
+__global__ void tex_peak_kernel(cudaTextureObject_t tex, int layers, int w, int h, int iters, float *sink)
+{
+    const int lane = threadIdx.x & 31, half = lane >> 4, c = lane & 15;
+    const unsigned gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    float acc = 0.0f;
+    unsigned s = gw * 2654435761u + 12345u;
+    for (int it = 0; it < iters; ++it) {
+        s = s * 1664525u + 1013904223u;
+        const float x0 = 20.0f + (float)((s >> 8) % (unsigned)(w - 60)) + 0.37f * half;
+        const float y0 = 20.0f + (float)((s >> 4) % (unsigned)(h - 60)) + 0.21f;
+        const int layer = (int)((s >> 20) % (unsigned)layers);
+#pragma unroll
+        for (int r = 0; r < 15; ++r)
+            acc += tex2DLayered<float>(tex, x0 + 1.003f * c + 0.013f * r, y0 + 0.997f * r, layer);
+    }
+    if (acc == -1.0f) sink[0] = acc;  // keeps the fetches; never true for these texels
+}
+
+cudaError_t measure_texture_peak(double *samples_per_s)
+{
+    const int W = 1280, H = 720, L = 10, threads = 256, iters = 200;
+    int sms = 0;
+    cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+    if (e != cudaSuccess) return e;
+    cudaArray_t arr = nullptr;
+    const cudaChannelFormatDesc cd = cudaCreateChannelDesc<uint8_t>();
+    e = cudaMalloc3DArray(&arr, &cd, make_cudaExtent(W, H, L), cudaArrayLayered);
+    if (e != cudaSuccess) return e;
+    cudaTextureObject_t tex = 0;
+    float *sink = nullptr;
+    cudaEvent_t a = nullptr, b = nullptr;
+    cudaResourceDesc rd{};
+    rd.resType = cudaResourceTypeArray;
+    rd.res.array.array = arr;
+    cudaTextureDesc td{};
+    td.addressMode[0] = td.addressMode[1] = cudaAddressModeBorder;
+    td.filterMode = cudaFilterModeLinear;
+    td.readMode = cudaReadModeNormalizedFloat;
+    e = cudaCreateTextureObject(&tex, &rd, &td, nullptr);
+    if (e == cudaSuccess) e = cudaMalloc(&sink, sizeof(float));
+    if (e == cudaSuccess) e = cudaEventCreate(&a);
+    if (e == cudaSuccess) e = cudaEventCreate(&b);
+    const int blocks = sms * 16;
+    if (e == cudaSuccess) {
+        tex_peak_kernel<<<blocks, threads>>>(tex, L, W, H, 5, sink);
+        e = cudaEventRecord(a);
+    }
+    if (e == cudaSuccess) {
+        tex_peak_kernel<<<blocks, threads>>>(tex, L, W, H, iters, sink);
+        e = cudaEventRecord(b);
+    }
+    if (e == cudaSuccess) e = cudaEventSynchronize(b);
+    float ms = 0.0f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+    if (e == cudaSuccess) *samples_per_s = (double)blocks * threads * iters * 15 / (ms * 1e-3);
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+    if (sink) cudaFree(sink);
+    if (tex) cudaDestroyTextureObject(tex);
+    cudaFreeArray(arr);
+    return e;
+}
+
 }  // namespace pm

@@ -343,3 +343,15 @@ def test_sweep_lockstep_local_search(small_scene, direction, parity_log):
     assert events / decisions <= 2e-4, f"{events} divergences in {decisions} decisions"
     assert changed > 0.05
     eng.close()
+
+
+def test_texture_peak_is_plausible(engine_lib):
+    """The measured texture-filtering rate the bench reports the sweep kernel against: between
+    1 and 5 bilinear samples per clock per SM."""
+    import ctypes as C
+    import torch
+    r = C.c_double(0.0)
+    assert engine_lib.pm_texture_peak(C.byref(r)) == 0
+    props = torch.cuda.get_device_properties(0)
+    per_sm_clk = r.value / (props.multi_processor_count * 2.07e9)
+    assert 1.0 <= per_sm_clk <= 5.0, per_sm_clk
