@@ -14,6 +14,7 @@ All compute runs in the CUDA engine (lib/libpatchmatch_gb300.so) through its C A
 from __future__ import annotations
 
 import ctypes as C
+import math
 from pathlib import Path
 from typing import Sequence
 
@@ -26,7 +27,7 @@ from ._native import (DIR_BOTTOM_TO_TOP, DIR_LEFT_TO_RIGHT, DIR_RIGHT_TO_LEFT, D
                       PmView)
 
 __all__ = [
-    "Image", "PatchMatch", "Engine", "Batch", "run_batch", "read_middlebury", "read_pnm", "write_pgm", "default_params",
+    "Image", "PatchMatch", "Engine", "Batch", "run_batch", "read_middlebury", "read_nvm", "read_pnm", "write_pgm", "default_params",
     "load_depth_file", "PatchMatchError", "PREFILTER_NONE", "PREFILTER_BOX", "PREFILTER_GAUSSIAN",
     "PRECISION_FP32", "PRECISION_MIXED", "DIR_LEFT_TO_RIGHT", "DIR_TOP_TO_BOTTOM",
     "DIR_RIGHT_TO_LEFT", "DIR_BOTTOM_TO_TOP", "INIT_RANDOM", "INIT_PROPOSAL",
@@ -115,6 +116,80 @@ def read_middlebury(path) -> list[Image]:
             p = path.parent / name
         out.append(Image(np.array(vals[0:9]), np.array(vals[9:18]), np.array(vals[18:21]), read_pnm(p)))
     return out
+
+
+def read_nvm(path) -> tuple[list[Image], list[tuple[float, float] | None]]:
+    """readNVM (image.cpp:130-245) with the per-camera depth ranges returned (the reference
+    fills a by-value copy and loses them). 'NVM_V3', the camera count (> 1), per camera
+    '<file> f qw qx qy qz cx cy cz d0 d1' (quaternion to R as image.cpp:95-118, T = -R C as
+    image.cpp:122-128, K = [f 0 W/2; 0 f H/2; 0 0 1]), then the 3D points, each
+    'x y z r g b n' followed by n projections 'camera feature u v'. A camera's range spans
+    the positive depths of the points it sees, widened by a quarter of its size on both sides
+    (the near side by less while it would reach zero, image.cpp:222-235); a camera that sees
+    no point has None. Raises ValueError for a file that is not NVM_V3."""
+    path = Path(path)
+    toks = path.read_text().split()
+    if not toks or not toks[0].startswith("NVM_V3"):
+        raise ValueError(f"{path}: not an NVM_V3 file")
+    ncam = int(toks[1])
+    if ncam <= 1:
+        raise ValueError(f"{path}: an NVM_V3 file needs at least two cameras")
+    out, i = [], 2
+    for _ in range(ncam):
+        name = toks[i]
+        f = float(toks[i + 1])
+        q = [float(x) for x in toks[i + 2:i + 6]]
+        c = [float(x) for x in toks[i + 6:i + 9]]
+        i += 11
+        # scalar double arithmetic in the reference's order, so the C++ reader agrees bit for bit
+        qq = math.sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3])
+        w, x, y, z = (q[0] / qq, q[1] / qq, q[2] / qq, q[3] / qq) if qq > 0 else (1.0, 0.0, 0.0, 0.0)
+        R = [w * w + x * x - z * z - y * y, 2 * x * y - 2 * z * w, 2 * y * w + 2 * z * x,
+             2 * x * y + 2 * w * z, y * y + w * w - z * z - x * x, 2 * z * y - 2 * x * w,
+             2 * x * z - 2 * y * w, 2 * y * z + 2 * w * x, z * z + w * w - y * y - x * x]
+        T = [-(R[3 * r] * c[0] + R[3 * r + 1] * c[1] + R[3 * r + 2] * c[2]) for r in range(3)]
+        p = Path(name)
+        if not p.exists():
+            p = path.parent / name
+        img = read_pnm(p)
+        h, wd = img.shape
+        K = np.array([[f, 0.0, wd / 2.0], [0.0, f, h / 2.0], [0.0, 0.0, 1.0]])
+        out.append(Image(K, R, T, img))
+    npoint = int(toks[i])
+    i += 1
+    if npoint <= 0:
+        raise ValueError(f"{path}: no 3D points")
+    lo = np.full(ncam, np.inf, np.float32)
+    hi = np.full(ncam, -np.inf, np.float32)
+    for _ in range(npoint):
+        pt = [float(np.float32(v)) for v in toks[i:i + 3]]
+        npj = int(toks[i + 6])
+        i += 7
+        for _ in range(npj):
+            cidx = int(toks[i])
+            i += 4
+            if not 0 <= cidx < ncam:
+                raise ValueError(f"{path}: projection names camera {cidx} of {ncam}")
+            im = out[cidx]
+            r2 = [float(v) for v in im.R[2]]
+            depth = np.float32(r2[0] * pt[0] + r2[1] * pt[1] + r2[2] * pt[2] + float(im.T[2]))
+            if depth <= 0:
+                continue
+            lo[cidx] = min(lo[cidx], depth)
+            hi[cidx] = max(hi[cidx], depth)
+    ranges: list[tuple[float, float] | None] = []
+    for a, b in zip(lo, hi):
+        if a > b:
+            ranges.append(None)
+            continue
+        size = np.float32(b - a)
+        ratio = np.float32(0.25)
+        near = np.float32(a - ratio * size)
+        while near <= 0:
+            ratio = np.float32(ratio / np.float32(1.1))
+            near = np.float32(a - ratio * size)
+        ranges.append((float(near), float(np.float32(b + np.float32(0.25) * size))))
+    return out, ranges
 
 
 def write_middlebury(path, names: Sequence[str], images: Sequence[Image]) -> None:

@@ -81,7 +81,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> dict[str, Path]:
         _run([nvcc, *ARCH, "-shared", "-o", str(engine), *map(str, objs)])
     cli = LIB / "pm_cli"
     if _stale(cli, [CSRC / "pm_cli.cpp", engine, scene_so, INCLUDE / "patchmatch_gb300.h"]):
-        _run(["g++", "-O2", "-std=c++17", "-I", str(INCLUDE), "-o", str(cli), str(CSRC / "pm_cli.cpp"),
+        _run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I", str(INCLUDE), "-o", str(cli), str(CSRC / "pm_cli.cpp"),
               f"-L{LIB}", "-lpatchmatch_gb300", f"-Wl,-rpath,{LIB}"])
     return {"engine": engine, "scene": scene_so, "cli": cli}
 

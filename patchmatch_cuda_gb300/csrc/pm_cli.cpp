@@ -4,9 +4,14 @@
 // (image.cpp:64-93: count, then per image "<file> K(9) R(9) t(3)"), PGM/PPM images (no
 // OpenCV; colour is converted with BT.601 luma weights like cvtColor BGR2GRAY), runs the
 // engine and writes outputFileName in the reference's depth format. blockDim_x/y are fixed
-// by the engine. NVM input is not supported (the reference's NVM path discards its depth
-// ranges, image.cpp:130 takes them by value).
+// by the engine. An NVM_V3 file (image.cpp:130-245) is read first, as the reference's main
+// does: cameras from focal length, quaternion and centre (principal point at the image
+// centre), and the reference image's depth range from the projected 3D points, widened by 25 %
+// (the reference computes those ranges into a by-value copy and loses them; here they reach
+// the engine).
+#include <algorithm>
 #include <cctype>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <fstream>
@@ -107,6 +112,115 @@ bool file_exists(const std::string &p)
     return (bool)f;
 }
 
+// Image::readNVM (image.cpp:130-245) with its depth ranges returned. Quaternion (w, x, y, z)
+// to rotation as image.cpp:95-118; T = -R C (image.cpp:122-128); K = [f 0 W/2; 0 f H/2; 0 0 1].
+bool read_nvm(const std::string &list, std::vector<Image> &imgs, std::vector<pm_view> &views,
+              std::vector<std::pair<float, float>> &ranges)
+{
+    std::ifstream in(list);
+    if (!in || in.peek() != 'N') return false;
+    std::string header;
+    in >> header;
+    if (header.find("NVM_V3") == std::string::npos) return false;
+    int ncam = 0;
+    in >> ncam;
+    if (!in || ncam <= 1) return false;
+    imgs.assign((size_t)ncam, Image());
+    views.assign((size_t)ncam, pm_view());
+    std::vector<double> Rd((size_t)ncam * 9), Td((size_t)ncam * 3);
+    for (int i = 0; i < ncam; ++i) {
+        std::string name;
+        double f, q[4], c[3], d[2];
+        in >> name >> f >> q[0] >> q[1] >> q[2] >> q[3] >> c[0] >> c[1] >> c[2] >> d[0] >> d[1];
+        if (!in) return false;
+        const double qq = std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+        double w = 1, x = 0, y = 0, z = 0;
+        if (qq > 0) { w = q[0] / qq; x = q[1] / qq; y = q[2] / qq; z = q[3] / qq; }
+        double *R = &Rd[(size_t)i * 9], *T = &Td[(size_t)i * 3];
+        R[0] = w * w + x * x - z * z - y * y; R[1] = 2 * x * y - 2 * z * w; R[2] = 2 * y * w + 2 * z * x;
+        R[3] = 2 * x * y + 2 * w * z; R[4] = y * y + w * w - z * z - x * x; R[5] = 2 * z * y - 2 * x * w;
+        R[6] = 2 * x * z - 2 * y * w; R[7] = 2 * y * z + 2 * w * x; R[8] = z * z + w * w - y * y - x * x;
+        for (int r = 0; r < 3; ++r) T[r] = -(R[3 * r] * c[0] + R[3 * r + 1] * c[1] + R[3 * r + 2] * c[2]);
+        const std::string path = file_exists(name) ? name : dir_of(list) + "/" + name;
+        if (!read_pnm(path, imgs[(size_t)i])) {
+            std::printf("cannot read image %s (PGM/PPM, 8-bit)\n", path.c_str());
+            return false;
+        }
+        pm_view &v = views[(size_t)i];
+        v.gray = imgs[(size_t)i].px.data();
+        v.width = v.stride = imgs[(size_t)i].w;
+        v.height = imgs[(size_t)i].h;
+        const float K[9] = {(float)f, 0.0f, (float)v.width / 2.0f, 0.0f, (float)f, (float)v.height / 2.0f,
+                            0.0f, 0.0f, 1.0f};
+        for (int k = 0; k < 9; ++k) { v.K[k] = K[k]; v.R[k] = (float)R[k]; }
+        for (int k = 0; k < 3; ++k) v.t[k] = (float)T[k];
+    }
+    ranges.assign((size_t)ncam, std::make_pair(3.402823466e+38f, -3.402823466e+38f));
+    int npoint = 0;
+    in >> npoint;
+    if (!in || npoint <= 0) return false;
+    for (int i = 0; i < npoint; ++i) {
+        float pt[3];
+        int col[3], npj;
+        in >> pt[0] >> pt[1] >> pt[2] >> col[0] >> col[1] >> col[2] >> npj;
+        if (!in) return false;
+        for (int j = 0; j < npj; ++j) {
+            int cidx, fidx;
+            float imx, imy;
+            in >> cidx >> fidx >> imx >> imy;
+            if (!in || cidx < 0 || cidx >= ncam) return false;
+            // depth = third row of K [R | T] applied to the point (K's third row is 0 0 1)
+            const pm_view &v = views[(size_t)cidx];
+            const float depth = (float)((double)v.R[6] * pt[0] + (double)v.R[7] * pt[1] +
+                                        (double)v.R[8] * pt[2] + (double)v.t[2]);
+            if (depth <= 0) continue;  // image.cpp:211-212
+            ranges[(size_t)cidx].first = std::min(ranges[(size_t)cidx].first, depth);
+            ranges[(size_t)cidx].second = std::max(ranges[(size_t)cidx].second, depth);
+        }
+    }
+    for (auto &r : ranges) {  // widen (image.cpp:222-235)
+        if (r.first > r.second) continue;  // camera without projections
+        const float size = r.second - r.first;
+        float ratio = 0.25f, near_ = r.first - ratio * size;
+        while (near_ <= 0) {
+            ratio /= 1.1f;
+            near_ = r.first - ratio * size;
+        }
+        r.first = near_;
+        r.second += 0.25f * size;
+    }
+    return true;
+}
+
+bool read_middlebury(const std::string &list, std::vector<Image> &imgs, std::vector<pm_view> &views)
+{
+    std::ifstream in(list);
+    if (!in) return false;
+    int n = 0;
+    in >> n;
+    if (n < 1) return false;
+    imgs.assign((size_t)n, Image());
+    views.assign((size_t)n, pm_view());
+    for (int i = 0; i < n; ++i) {
+        std::string name;
+        pm_view &v = views[(size_t)i];
+        in >> name;
+        for (float &k : v.K) in >> k;
+        for (float &r : v.R) in >> r;
+        for (float &t : v.t) in >> t;
+        if (!in) return false;
+        std::string path = file_exists(name) ? name : dir_of(list) + "/" + name;
+        if (!read_pnm(path, imgs[(size_t)i])) {
+            std::printf("cannot read image %s (PGM/PPM, 8-bit)\n", path.c_str());
+            return false;
+        }
+        v.gray = imgs[(size_t)i].px.data();
+        v.width = v.stride = imgs[(size_t)i].w;
+        v.height = imgs[(size_t)i].h;
+    }
+    return true;
+}
+
 }  // namespace
 
 int main(int argc, char **argv)
@@ -151,40 +265,25 @@ int main(int argc, char **argv)
     const std::string out = get("outputFileName");
 
     const std::string list = get("imageInfoFileName");
-    std::ifstream in(list);
-    if (!in) {
+    std::vector<Image> imgs;
+    std::vector<pm_view> views;
+    std::vector<std::pair<float, float>> ranges;
+    if (read_nvm(list, imgs, views, ranges)) {
+        if (ref_id < 0 || ref_id >= (int)ranges.size() || ranges[(size_t)ref_id].first > ranges[(size_t)ref_id].second) {
+            std::printf("NVM file has no 3D point seen by image %d\n", ref_id);
+            return 1;
+        }
+        // main.cpp:117-121: the NVM range of the reference image replaces the configured one
+        p.depth_near = ranges[(size_t)ref_id].first;
+        p.depth_far = ranges[(size_t)ref_id].second;
+        std::printf("using NVM files: depth range [%.9g, %.9g] for image %d\n", p.depth_near, p.depth_far, ref_id);
+    } else if (read_middlebury(list, imgs, views)) {
+        std::printf("using Middlebury files\n");
+    } else {
         std::printf("cannot parse image files\n");
         return 1;
     }
-    int n = 0;
-    in >> n;
-    if (n < 1) {
-        std::printf("cannot parse image files\n");
-        return 1;
-    }
-    std::vector<Image> imgs((size_t)n);
-    std::vector<pm_view> views((size_t)n);
-    for (int i = 0; i < n; ++i) {
-        std::string name;
-        pm_view &v = views[(size_t)i];
-        in >> name;
-        for (float &k : v.K) in >> k;
-        for (float &r : v.R) in >> r;
-        for (float &t : v.t) in >> t;
-        if (!in) {
-            std::printf("cannot parse image files\n");
-            return 1;
-        }
-        std::string path = file_exists(name) ? name : dir_of(list) + "/" + name;
-        if (!read_pnm(path, imgs[(size_t)i])) {
-            std::printf("cannot read image %s (PGM/PPM, 8-bit)\n", path.c_str());
-            return 1;
-        }
-        v.gray = imgs[(size_t)i].px.data();
-        v.width = v.stride = imgs[(size_t)i].w;
-        v.height = imgs[(size_t)i].h;
-    }
-    std::printf("using Middlebury files\n");
+    const int n = (int)views.size();
 
     pm_handle *h = nullptr;
     pm_status s = pm_create(views.data(), n, ref_id, &p, &h);

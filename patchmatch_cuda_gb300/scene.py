@@ -19,6 +19,7 @@ from __future__ import annotations
 
 import ctypes as C
 from dataclasses import dataclass, field
+from pathlib import Path
 
 import numpy as np
 
@@ -210,3 +211,64 @@ def bad_pixel_rate(depth: np.ndarray, gt: np.ndarray, rel: float = 0.01) -> floa
     valid = gt > 0
     err = np.abs(depth[valid] - gt[valid]) / gt[valid]
     return float(np.mean(err > rel))
+
+
+def rotation_to_quaternion(R) -> tuple[float, float, float, float]:
+    """(w, x, y, z) of a rotation matrix (Shepperd's method), the inverse of the NVM reader's
+    quaternion-to-rotation formula."""
+    R = np.asarray(R, np.float64).reshape(3, 3)
+    tr = R[0, 0] + R[1, 1] + R[2, 2]
+    if tr > 0:
+        s = 2.0 * np.sqrt(tr + 1.0)
+        return 0.25 * s, (R[2, 1] - R[1, 2]) / s, (R[0, 2] - R[2, 0]) / s, (R[1, 0] - R[0, 1]) / s
+    i = int(np.argmax(np.diag(R)))
+    j, k = (i + 1) % 3, (i + 2) % 3
+    s = 2.0 * np.sqrt(1.0 + R[i, i] - R[j, j] - R[k, k])
+    q = [0.0, 0.0, 0.0]
+    q[i] = 0.25 * s
+    q[j] = (R[j, i] + R[i, j]) / s
+    q[k] = (R[k, i] + R[i, k]) / s
+    return (R[k, j] - R[j, k]) / s, q[0], q[1], q[2]
+
+
+def write_nvm(path, names, images, points, visible=None) -> None:
+    """An NVM_V3 model of calibrated views: per camera its file, focal length K[0][0],
+    quaternion and centre -R^T T (the reader puts the principal point at the image centre),
+    then the 3D points [n, 3], each with its projection into every camera it lies in front
+    of (visible[i] lists the cameras of point i where given)."""
+    lines = ["NVM_V3", "", str(len(images))]
+    for name, im in zip(names, images):
+        R = np.asarray(im.R, np.float64)
+        c = -R.T @ np.asarray(im.T, np.float64)
+        q = rotation_to_quaternion(R)
+        lines.append(" ".join([name, repr(float(im.K[0, 0]))] + [repr(float(v)) for v in q] +
+                              [repr(float(v)) for v in c] + ["0", "0"]))
+    pts = np.asarray(points, np.float64).reshape(-1, 3)
+    lines += ["", str(len(pts))]
+    for i, p in enumerate(pts):
+        cams = range(len(images)) if visible is None else visible[i]
+        proj = []
+        for cidx in cams:
+            im = images[cidx]
+            u = np.asarray(im.K, np.float64) @ (np.asarray(im.R, np.float64) @ p + np.asarray(im.T, np.float64))
+            if visible is None and u[2] <= 0:
+                continue
+            proj.append(f"{cidx} {i} {u[0] / u[2]:.3f} {u[1] / u[2]:.3f}")
+        lines.append(" ".join([repr(float(v)) for v in p] + ["128", "128", "128", str(len(proj))] + proj))
+    lines += ["", "0", ""]
+    Path(path).write_text("\n".join(lines))
+
+
+def nvm_points(sv: SceneViews, step: int = 8) -> np.ndarray:
+    """3D points of the reference's ground truth on a pixel grid (a stand-in for a structure
+    from motion point cloud)."""
+    im = sv.images[sv.ref_id]
+    K, R, T = (np.asarray(a, np.float64) for a in (im.K, im.R, im.T))
+    h, w = sv.gt_depth.shape
+    ys, xs = np.mgrid[step // 2:h:step, step // 2:w:step]
+    d = sv.gt_depth[ys, xs].astype(np.float64)
+    keep = d > 0
+    pix = np.stack([xs[keep] + 0.5, ys[keep] + 0.5, np.ones(int(keep.sum()))], axis=0)
+    cam = np.linalg.solve(K, pix) * d[keep]
+    return (R.T @ (cam - T[:, None])).T
+

@@ -116,6 +116,36 @@ def test_cli_matches_the_library(small, tmp_path):
     eng.close()
 
 
+def test_cli_on_an_nvm_model_matches_the_library(small, tmp_path):
+    """An NVM_V3 model through the CLI (cameras and the reference's depth range from the file)
+    gives the depth map of the library run on read_nvm's views and range."""
+    from patchmatch_cuda_gb300 import Engine, _native, load_depth_file, read_nvm, scene, write_pgm
+    names = []
+    for i, im in enumerate(small.images):
+        write_pgm(tmp_path / f"v{i}.pgm", im.image)
+        names.append(f"v{i}.pgm")
+    scene.write_nvm(tmp_path / "model.nvm", names, small.images, scene.nvm_points(small, step=6))
+    w = small.workload
+    (tmp_path / "run.ini").write_text(
+        "[params]\n"
+        f"imageInfoFileName = {tmp_path / 'model.nvm'}\n"
+        f"refImageId = {small.ref_id}\nhalfWindowSize = {w.half_window}\nnumOfSamples = {w.num_samples}\n"
+        f"SPMAlpha = {w.sp_alpha}\ngaussianSigma = {w.gaussian_sigma}\nnumOfIterations = {w.iterations}\n"
+        f"outputFileName = {tmp_path / 'depth.bin'}\nprefilter = {w.prefilter}\nseed = {w.seed}\n")
+    r = subprocess.run([str(_native.LIB_DIR / "pm_cli"), str(tmp_path / "run.ini")], capture_output=True,
+                       text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    imgs, ranges = read_nvm(tmp_path / "model.nvm")
+    near, far = ranges[small.ref_id]
+    eng = Engine(imgs, small.ref_id, w.params(depth_near=near, depth_far=far))
+    eng.run()
+    d = eng.depth()
+    np.testing.assert_array_equal(load_depth_file(tmp_path / "depth.bin"), d)
+    eng.close()
+    gt = small.gt_depth
+    assert scene.bad_pixel_rate(d, gt, 0.05) < 0.5             # the NVM cameras reconstruct the scene
+
+
 def test_reference_mirror_class(small):
     from patchmatch_cuda_gb300 import PatchMatch
     w = small.workload

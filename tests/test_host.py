@@ -135,3 +135,98 @@ def test_replica_aggregation_over_gloo():
         p.join(timeout=60)
     assert [r[1] for r in res] == [11.0, 11.0]
     assert [r[2] for r in res] == [300.0, 300.0]
+
+
+def _nvm_scene(tmp_path, n_views=3):
+    from patchmatch_cuda_gb300 import scene, write_pgm
+    w = scene.Workload("nvm_96x64", 96, 64, n_views - 1, 2, 1, 2.0, 8.0, 3, 0, seed=5)
+    sv = scene.make_views(w)
+    names = []
+    for i, im in enumerate(sv.images):
+        write_pgm(tmp_path / f"c{i}.pgm", im.image)
+        names.append(f"c{i}.pgm")
+    return sv, names
+
+
+def _loosened(lo, hi):
+    """The widening rule of image.cpp:222-235 in float32."""
+    lo, hi = np.float32(lo), np.float32(hi)
+    size = np.float32(hi - lo)
+    ratio = np.float32(0.25)
+    near = np.float32(lo - ratio * size)
+    while near <= 0:
+        ratio = np.float32(ratio / np.float32(1.1))
+        near = np.float32(lo - ratio * size)
+    return float(near), float(np.float32(hi + np.float32(0.25) * size))
+
+
+def test_nvm_reader_cameras_and_depth_ranges(tmp_path):
+    from patchmatch_cuda_gb300 import read_nvm, scene
+    sv, names = _nvm_scene(tmp_path)
+    pts = scene.nvm_points(sv)
+    behind = sv.images[0].C.astype(np.float64) - 3.0 * sv.images[0].R[2].astype(np.float64)
+    pts_all = np.concatenate([pts, behind[None]], axis=0)          # one point behind camera 0
+    vis = [list(range(3))] * len(pts) + [[0]]
+    scene.write_nvm(tmp_path / "model.nvm", names, sv.images, pts_all, visible=vis)
+    imgs, ranges = read_nvm(tmp_path / "model.nvm")
+    assert len(imgs) == 3 and len(ranges) == 3
+    for a, b in zip(imgs, sv.images):
+        h, w = b.image.shape
+        np.testing.assert_array_equal(a.image, b.image)
+        np.testing.assert_allclose(a.R, b.R, atol=1e-6)
+        np.testing.assert_allclose(a.T, b.T, rtol=1e-6, atol=1e-6)
+        np.testing.assert_array_equal(a.K, np.array([[b.K[0, 0], 0, w / 2], [0, b.K[0, 0], h / 2], [0, 0, 1]],
+                                                     np.float32))
+    for a, im in zip(ranges, imgs):
+        z = (pts.astype(np.float32).astype(np.float64) @ im.R[2].astype(np.float64)) + float(im.T[2])
+        want = _loosened(np.float32(z.min()), np.float32(z.max()))
+        np.testing.assert_allclose(a, want, rtol=2e-7)
+        assert 0 < a[0] < z.min() and a[1] > z.max()
+
+
+def test_nvm_reader_edge_cases(tmp_path):
+    from patchmatch_cuda_gb300 import read_nvm, scene
+    sv, names = _nvm_scene(tmp_path)
+    pts = scene.nvm_points(sv, step=16)
+    scene.write_nvm(tmp_path / "m.nvm", names, sv.images, pts, visible=[[0, 1]] * len(pts))
+    _, ranges = read_nvm(tmp_path / "m.nvm")
+    assert ranges[2] is None and ranges[0] is not None           # camera 2 sees no point
+    # the near side shrinks its margin while it would reach zero
+    lo, hi = 1.0, 9.0
+    near, far = _loosened(lo, hi)
+    assert 0 < near < lo and far == 11.0
+    (tmp_path / "one.nvm").write_text("NVM_V3\n1\nc0.pgm 100 1 0 0 0 0 0 0 0 0\n1\n0 0 5 1 1 1 1 0 0 1 1\n")
+    with pytest.raises(ValueError, match="two cameras"):
+        read_nvm(tmp_path / "one.nvm")
+    (tmp_path / "mb.txt").write_text("1\nc0.pgm" + " 0" * 21 + "\n")
+    with pytest.raises(ValueError, match="not an NVM_V3"):
+        read_nvm(tmp_path / "mb.txt")
+
+
+def test_cli_reads_nvm_and_uses_its_depth_range(tmp_path):
+    """main.cpp:98-121: the list is tried as NVM first, and the reference image's NVM range
+    replaces the configured one. Without a GPU the run stops at engine creation, after the
+    range is printed."""
+    import re
+    from patchmatch_cuda_gb300 import read_nvm, scene
+    cli = _cli()
+    if not cli.exists():
+        pytest.skip("CLI not built")
+    sv, names = _nvm_scene(tmp_path)
+    pts = scene.nvm_points(sv)
+    scene.write_nvm(tmp_path / "model.nvm", names, sv.images, pts, visible=[[0, 1, 2]] * (len(pts) - 1) + [[0, 1]])
+    _, ranges = read_nvm(tmp_path / "model.nvm")
+    ini = ("[params]\nimageInfoFileName = {}\nrefImageId = {}\nhalfWindowSize = 2\nnumOfSamples = 1\n"
+           "SPMAlpha = 0.45\ngaussianSigma = 1\nnumOfIterations = 1\noutputFileName = {}\n")
+    for ref in (1, 2):
+        (tmp_path / "c.ini").write_text(ini.format(tmp_path / "model.nvm", ref, tmp_path / "d.bin"))
+        r = subprocess.run([str(cli), str(tmp_path / "c.ini")], capture_output=True, text=True, timeout=60)
+        m = re.search(r"using NVM files: depth range \[([^,]+), ([^\]]+)\] for image (\d+)", r.stdout)
+        assert m, r.stdout
+        assert int(m.group(3)) == ref
+        assert (np.float32(m.group(1)), np.float32(m.group(2))) == (np.float32(ranges[ref][0]),
+                                                                    np.float32(ranges[ref][1]))
+    scene.write_nvm(tmp_path / "m2.nvm", names, sv.images, pts, visible=[[0, 1]] * len(pts))
+    (tmp_path / "c.ini").write_text(ini.format(tmp_path / "m2.nvm", 2, tmp_path / "d.bin"))
+    r = subprocess.run([str(cli), str(tmp_path / "c.ini")], capture_output=True, text=True, timeout=60)
+    assert r.returncode != 0 and "no 3D point seen by image 2" in r.stdout
