@@ -330,6 +330,62 @@ pm_status pm_net_train_step(pm_net *net, const float *d_input, const float *d_ta
  * input width). */
 pm_status pm_net_layout(const pm_net *net, int *n_layers, int *desc, int max_layers);
 
+/* ---- Consistency filtering and fusion over several references (no counterpart in the
+ * reference, whose output stops at one depth map per run: patchMatch.cu:263-407,
+ * main.cpp:124-128). All references share one world frame.
+ *
+ * For pixel (x, y) of reference i with depth d and every other reference j: the pixel centre
+ * (x + 1/2, y + 1/2) at depth d is projected into j, j's depth at the pixel containing the
+ * projection is projected back into i, and j agrees when that round trip lands within
+ * max_reproj_px pixels of the start with a depth within max_rel_depth * d of d. Pixels with
+ * at least min_consistent agreeing references are kept, with the mean of d and the agreeing
+ * round-trip depths as their fused depth and its back-projection as their point. Depths that
+ * are not finite and positive count as missing. */
+#define PM_MAX_FUSE_REFS 256
+
+typedef struct pm_fuse_params {
+    float max_reproj_px;        /* default 1                                                */
+    float max_rel_depth;        /* default 0.01                                             */
+    int min_consistent;         /* other references that must agree (default 2; 0 keeps
+                                   every valid depth)                                       */
+} pm_fuse_params;
+void pm_default_fuse_params(pm_fuse_params *p);
+
+/* One reference's depth map with its camera, on the host. */
+typedef struct pm_depth_view {
+    const float *depth;         /* height rows of width floats                               */
+    const uint8_t *gray;        /* intensity for the points, same size, or NULL (0)          */
+    int width, height;
+    float K[9], R[9], t[3];     /* row-major, pixel ~ K (R X + t)                             */
+} pm_depth_view;
+
+typedef struct pm_fusion pm_fusion;
+/* Copies host depth maps to the device (gpu_id < 0: the current device). */
+pm_status pm_fusion_create(const pm_depth_view *views, int n, int gpu_id, pm_fusion **out);
+/* Reads the engines' device depth maps in place at every pm_fusion_run (after synchronising
+ * their streams), with each engine's reference texels as intensity. The engines must outlive
+ * the fusion object and have a depth map (run, initialised or set). */
+pm_status pm_fusion_create_from_engines(pm_handle *const *hs, int n, pm_fusion **out);
+/* Filters and fuses; synchronous. May run again (e.g. after the engines ran again). */
+pm_status pm_fusion_run(pm_fusion *f, const pm_fuse_params *p);
+/* Points of the last run, the device time of the consistency kernel and of the whole fusion
+ * (CUDA events, ms), and the kernels one run launches. */
+pm_status pm_fusion_info(const pm_fusion *f, int64_t *num_points, float *ms_check, float *ms_total,
+                         int *launches);
+/* Up to capacity points as (x, y, z, intensity in [0, 1]), reference by reference in row-major
+ * pixel order. */
+pm_status pm_fusion_get_points(pm_fusion *f, float *xyzi, int64_t capacity);
+/* Reference ref's fused depth (0 where not kept) and per-pixel count of agreeing references
+ * (either may be NULL). */
+pm_status pm_fusion_get_depth(pm_fusion *f, int ref, float *fused, uint8_t *count);
+/* The FP32 matrices the kernels use: pairs[(i n + j) 12 ..] = K_j R_j R_i^T K_i^-1 (row-major)
+ * then K_j (t_j - R_j R_i^T t_i); backproject[i 12 ..] = R_i^T K_i^-1 then -R_i^T t_i. */
+pm_status pm_fusion_geometry(const pm_fusion *f, float *pairs, float *backproject);
+/* Binary little-endian PLY: x y z (float), gray as red = green = blue (uchar). */
+pm_status pm_fusion_write_ply(pm_fusion *f, const char *path);
+const char *pm_fusion_last_error(const pm_fusion *f);
+pm_status pm_fusion_destroy(pm_fusion *f);
+
 #ifdef __cplusplus
 }
 #endif

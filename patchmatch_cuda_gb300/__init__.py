@@ -23,11 +23,11 @@ import numpy as np
 from . import _native
 from ._native import (DIR_BOTTOM_TO_TOP, DIR_LEFT_TO_RIGHT, DIR_RIGHT_TO_LEFT, DIR_TOP_TO_BOTTOM,
                       PRECISION_FP32, PRECISION_MIXED, PREFILTER_BOX, PREFILTER_GAUSSIAN,
-                      PREFILTER_NONE, INIT_PROPOSAL, INIT_RANDOM, PatchMatchError, PmParams, PmStats,
-                      PmView)
+                      PREFILTER_NONE, INIT_PROPOSAL, INIT_RANDOM, PatchMatchError, PmFuseParams, PmParams,
+                      PmStats, PmView)
 
 __all__ = [
-    "Image", "PatchMatch", "Engine", "Batch", "run_batch", "read_middlebury", "read_nvm", "read_pnm", "write_pgm", "default_params",
+    "Image", "PatchMatch", "Engine", "Batch", "Fusion", "default_fuse_params", "run_batch", "read_middlebury", "read_nvm", "read_pnm", "write_pgm", "default_params",
     "load_depth_file", "PatchMatchError", "PREFILTER_NONE", "PREFILTER_BOX", "PREFILTER_GAUSSIAN",
     "PRECISION_FP32", "PRECISION_MIXED", "DIR_LEFT_TO_RIGHT", "DIR_TOP_TO_BOTTOM",
     "DIR_RIGHT_TO_LEFT", "DIR_BOTTOM_TO_TOP", "INIT_RANDOM", "INIT_PROPOSAL",
@@ -386,6 +386,109 @@ class Batch:
     def close(self) -> None:
         if getattr(self, "h", None):
             self._lib.pm_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def default_fuse_params(**over) -> PmFuseParams:
+    """Consistency thresholds: max_reproj_px 1, max_rel_depth 0.01, min_consistent 2."""
+    p = PmFuseParams()
+    _native.load_engine().pm_default_fuse_params(C.byref(p))
+    for k, v in over.items():
+        setattr(p, k, v)
+    return p
+
+
+class Fusion:
+    """Consistency filtering and fusion of several references' depth maps (pm_fusion): no
+    counterpart in the reference, the step after the path.
+
+    Fusion(engines) reads the engines' device depth maps in place at every run;
+    Fusion.from_depth_maps(depths, images) copies host depth maps (with the Image cameras and
+    intensities) to the device."""
+
+    def __init__(self, engines: Sequence[Engine] | None = None, *, _handle=None, _sizes=None):
+        self._lib = _native.load_engine()
+        self.h = C.c_void_p()
+        if _handle is not None:
+            self.h = _handle
+            self.sizes = list(_sizes)
+        else:
+            self.engines = list(engines)
+            arr = (C.c_void_p * len(self.engines))(*[e.h for e in self.engines])
+            _native.check(self._lib.pm_fusion_create_from_engines(arr, len(self.engines), C.byref(self.h)))
+            self.sizes = [(e.height, e.width) for e in self.engines]
+        self.n = len(self.sizes)
+
+    @classmethod
+    def from_depth_maps(cls, depths: Sequence[np.ndarray], images: Sequence[Image], gpu_id: int = -1) -> "Fusion":
+        lib = _native.load_engine()
+        n = len(depths)
+        views = (_native.PmDepthView * n)()
+        keep = []   # alive until pm_fusion_create has copied them
+        for k, (d, im) in enumerate(zip(depths, images)):
+            d = np.ascontiguousarray(d, np.float32)
+            g = np.ascontiguousarray(im.image, np.uint8) if im.image is not None else None
+            v = views[k]
+            v.depth = d.ctypes.data
+            v.gray = g.ctypes.data if g is not None else None
+            v.height, v.width = d.shape
+            if g is not None and g.shape != d.shape:
+                raise ValueError("intensity image and depth map differ in size")
+            v.K[:] = [float(x) for x in im.K.ravel()]
+            v.R[:] = [float(x) for x in im.R.ravel()]
+            v.t[:] = [float(x) for x in im.T.ravel()]
+            keep.append((d, g))
+        h = C.c_void_p()
+        _native.check(lib.pm_fusion_create(views, n, gpu_id, C.byref(h)))
+        return cls(_handle=h, _sizes=[d.shape for d, _ in keep])
+
+    def _chk(self, st: int) -> None:
+        if st != 0:
+            raw = self._lib.pm_fusion_last_error(self.h)
+            raise PatchMatchError(st, raw.decode() if raw else "")
+
+    def run(self, params: PmFuseParams | None = None) -> int:
+        self._chk(self._lib.pm_fusion_run(self.h, C.byref(params or default_fuse_params())))
+        return self.info()["points"]
+
+    def info(self) -> dict:
+        n, t1, t2, l = C.c_int64(), C.c_float(), C.c_float(), C.c_int()
+        self._chk(self._lib.pm_fusion_info(self.h, C.byref(n), C.byref(t1), C.byref(t2), C.byref(l)))
+        return {"points": n.value, "ms_check": t1.value, "ms_total": t2.value, "launches": l.value}
+
+    def points(self) -> np.ndarray:
+        """(n, 4) float32: x, y, z and intensity in [0, 1]."""
+        n = self.info()["points"]
+        out = np.empty((n, 4), np.float32)
+        self._chk(self._lib.pm_fusion_get_points(self.h, out.ctypes.data, n))
+        return out
+
+    def depth(self, ref: int) -> tuple[np.ndarray, np.ndarray]:
+        """Fused depth (0 where not kept) and the count of agreeing references."""
+        h, w = self.sizes[ref]
+        fused = np.empty((h, w), np.float32)
+        count = np.empty((h, w), np.uint8)
+        self._chk(self._lib.pm_fusion_get_depth(self.h, ref, fused.ctypes.data, count.ctypes.data))
+        return fused, count
+
+    def geometry(self) -> tuple[np.ndarray, np.ndarray]:
+        pairs = np.empty((self.n, self.n, 12), np.float32)
+        bp = np.empty((self.n, 12), np.float32)
+        self._chk(self._lib.pm_fusion_geometry(self.h, pairs.ctypes.data, bp.ctypes.data))
+        return pairs, bp
+
+    def write_ply(self, path) -> None:
+        self._chk(self._lib.pm_fusion_write_ply(self.h, str(path).encode()))
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self._lib.pm_fusion_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -38,8 +38,13 @@ EXPORTED_SYMBOLS = [
     "pm_gemm_bf16", "pm_gemm_error", "pm_net_create", "pm_net_destroy", "pm_net_num_params",
     "pm_net_get_params", "pm_net_set_params", "pm_net_forward", "pm_net_gradients", "pm_net_train_step",
     "pm_net_layout", "pm_net_size", "pm_set_proposal", "pm_proposal_input", "pm_batch_create",
-    "pm_batch_run", "pm_batch_info", "pm_batch_destroy", "pm_texture_peak",
+    "pm_batch_run", "pm_batch_info", "pm_batch_destroy", "pm_texture_peak", "pm_default_fuse_params",
+    "pm_fusion_create", "pm_fusion_create_from_engines", "pm_fusion_run", "pm_fusion_info",
+    "pm_fusion_get_points", "pm_fusion_get_depth", "pm_fusion_geometry", "pm_fusion_write_ply",
+    "pm_fusion_last_error", "pm_fusion_destroy",
 ]
+
+MAX_FUSE_REFS = 256
 
 
 class PmView(C.Structure):
@@ -67,6 +72,17 @@ class PmStats(C.Structure):
         ("cost_evals", C.c_ulonglong), ("cost_evals_done", C.c_ulonglong),
         ("ms_prepare", C.c_float), ("ms_init", C.c_float), ("ms_sweeps", C.c_float),
         ("ms_total", C.c_float), ("threads_per_line", C.c_int), ("texel_bytes", C.c_int),
+    ]
+
+
+class PmFuseParams(C.Structure):
+    _fields_ = [("max_reproj_px", C.c_float), ("max_rel_depth", C.c_float), ("min_consistent", C.c_int)]
+
+
+class PmDepthView(C.Structure):
+    _fields_ = [
+        ("depth", C.c_void_p), ("gray", C.c_void_p), ("width", C.c_int), ("height", C.c_int),
+        ("K", C.c_float * 9), ("R", C.c_float * 9), ("t", C.c_float * 3),
     ]
 
 
@@ -138,6 +154,17 @@ def load_engine() -> C.CDLL:
         "pm_batch_info": (C.c_int, [P, P, P, P, C.c_int]),
         "pm_batch_destroy": (C.c_int, [P]),
         "pm_texture_peak": (C.c_int, [P]),
+        "pm_default_fuse_params": (None, [P]),
+        "pm_fusion_create": (C.c_int, [P, C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
+        "pm_fusion_create_from_engines": (C.c_int, [P, C.c_int, C.POINTER(C.c_void_p)]),
+        "pm_fusion_run": (C.c_int, [P, P]),
+        "pm_fusion_info": (C.c_int, [P, P, P, P, P]),
+        "pm_fusion_get_points": (C.c_int, [P, P, C.c_int64]),
+        "pm_fusion_get_depth": (C.c_int, [P, C.c_int, P, P]),
+        "pm_fusion_geometry": (C.c_int, [P, P, P]),
+        "pm_fusion_write_ply": (C.c_int, [P, C.c_char_p]),
+        "pm_fusion_last_error": (C.c_char_p, [P]),
+        "pm_fusion_destroy": (C.c_int, [P]),
         "pm_box_moments_noalloc": (C.c_int, [P, C.c_size_t, C.c_int, C.c_int, C.c_int, P, P, P, C.c_size_t, P]),
     }
     for name, (res, args) in sig.items():

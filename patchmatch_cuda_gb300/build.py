@@ -28,7 +28,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-Wa
 
 CUDA_SOURCES = ["pm_win_a.cu", "pm_win_b.cu", "pm_win_c.cu", "pm_win_d.cu", "pm_win_a_hw.cu", "pm_win_b_hw.cu",
                 "pm_win_c_hw.cu", "pm_win_d_hw.cu", "pm_prep.cu", "pm_api.cu", "pm_noalloc.cu", "pm_gemm.cu",
-                "pm_net.cu", "pm_proposal.cu"]
+                "pm_net.cu", "pm_proposal.cu", "pm_fuse.cu"]
 HEADERS = ["pm_device.cuh", "pm_sweep.cuh", "pm_internal.h", "pm_windows.inc"]
 
 

@@ -52,6 +52,8 @@ struct pm_handle {
     float *d_prop_in = nullptr, *d_prop_out = nullptr;
     cudaGraphExec_t graph = nullptr;
     bool ran = false;
+    bool has_depth = false;             // a depth map was initialised, set or computed
+    float cam_K[9] = {}, cam_R[9] = {}, cam_t[3] = {};   // the reference camera
     pm_stats stats{};
 };
 
@@ -540,6 +542,11 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
     h->H = ref.height;
     h->V = n_views - 1;
     h->win = 2 * p.half_window + 1;
+    for (int k = 0; k < 9; ++k) {
+        h->cam_K[k] = ref.K[k];
+        h->cam_R[k] = ref.R[k];
+    }
+    for (int k = 0; k < 3; ++k) h->cam_t[k] = ref.t[k];
     const bool filtered = p.prefilter != PM_PREFILTER_NONE;
     h->texel_bytes = p.texel_format != PM_TEXELS_AUTO ? p.texel_format
                      : p.precision == PM_PRECISION_FP32 ? (filtered ? 4 : 1) : (filtered ? 2 : 1);
@@ -839,6 +846,7 @@ pm_status pm_run_async(pm_handle *h)
     PM_CUDA(h, cudaGraphLaunch(h->graph, h->stream));
     PM_CUDA(h, cudaEventRecord(h->ev[3], h->stream));
     h->ran = true;
+    h->has_depth = true;
     return PM_OK;
 }
 
@@ -1036,6 +1044,7 @@ pm_status batch_finish(pm_batch *b)
         h->stats.cost_evals = ev[0];
         h->stats.cost_evals_done = ev[1];
         h->ran = true;
+        h->has_depth = true;
     }
     return PM_OK;
 }
@@ -1206,6 +1215,7 @@ pm_status pm_init_depth(pm_handle *h)
         PM_CUDA(h, launch_init_depth(h->d_desc, 0, h->W * h->H, h->stream));
     }
     PM_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->has_depth = true;
     return PM_OK;
 }
 
@@ -1262,7 +1272,35 @@ pm_status pm_set_depth(pm_handle *h, const float *src)
     if (st != PM_OK) return st;
     PM_CUDA(h, cudaMemcpyAsync(h->d_depth, src, (size_t)h->W * h->H * 4, cudaMemcpyHostToDevice, h->stream));
     PM_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->has_depth = true;
     return PM_OK;
+}
+
+pm_status pm_fusion_create_from_engines(pm_handle *const *hs, int n, pm_fusion **out)
+{
+    if (!out) return PM_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    if (!hs || n < 1 || n > PM_MAX_FUSE_REFS) return PM_ERR_INVALID_ARGUMENT;
+    std::vector<FuseSource> src((size_t)n);
+    for (int i = 0; i < n; ++i) {
+        const pm_handle *h = hs[i];
+        if (!h) return PM_ERR_INVALID_ARGUMENT;
+        if (h->device != hs[0]->device) return PM_ERR_INVALID_ARGUMENT;
+        if (!h->has_depth) return PM_ERR_STATE;
+        FuseSource &f = src[(size_t)i];
+        f = FuseSource{};
+        f.d_depth = h->d_depth;
+        f.d_intensity = h->d_ref;
+        f.width = h->W;
+        f.height = h->H;
+        for (int k = 0; k < 9; ++k) {
+            f.K[k] = h->cam_K[k];
+            f.R[k] = h->cam_R[k];
+        }
+        for (int k = 0; k < 3; ++k) f.t[k] = h->cam_t[k];
+        f.wait_stream = h->stream;
+    }
+    return fusion_create(src.data(), n, hs[0]->device, out);
 }
 
 pm_status pm_get_costs(pm_handle *h, float *dst)

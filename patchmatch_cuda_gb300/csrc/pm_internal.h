@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "patchmatch_gb300.h"
 #include "pm_sweep.cuh"
 
 namespace pm {
@@ -71,6 +72,20 @@ cudaError_t launch_philox(uint64_t seed, int n, const uint32_t *ctr, uint32_t *o
                           cudaStream_t s);
 cudaError_t launch_check_rcp(int exp_shift, unsigned long long *mismatches, cudaStream_t s);
 cudaError_t measure_texture_peak(double *samples_per_s);
+
+// Consistency filtering and fusion (pm_fuse.cu). A source's depth map is either on the device
+// already (an engine's, read in place after its stream is synchronised) or copied from the host
+// at creation.
+struct FuseSource {
+    const float *d_depth;        // device depth map, or null
+    const float *d_intensity;    // device intensity in [0, 1], or null
+    const float *h_depth;        // host depth map (when d_depth is null)
+    const uint8_t *h_gray;       // host intensity 0..255, or null
+    int width, height;
+    float K[9], R[9], t[3];
+    cudaStream_t wait_stream;    // synchronised before every run, or null
+};
+pm_status fusion_create(const FuseSource *sources, int n, int device, pm_fusion **out);
 
 // Learned proposal (pm_proposal.cu): quarter-resolution images, the plane-sweep input of the
 // network (17 channels), and the initial depth from its output.

@@ -206,6 +206,17 @@ def make_full_batch(n_refs: int = 8, seed: int = 55, width: int = 3072, height: 
     return out
 
 
+def scene_views(specs, seed: int = 7, n_planes: int = 4, n_boxes: int = 6, depth_near: float = 2.0,
+                depth_far: float = 8.0) -> list[tuple[Image, np.ndarray]]:
+    """Views of one scene, specs = [(yaw, pitch, width, height, focal)], each with its ground
+    truth z-depth (the references of a fusion)."""
+    w0, h0, f0 = specs[0][2], specs[0][3], specs[0][4]
+    sc = Scene(seed, n_planes, n_boxes, depth_near, depth_far, w0, h0, f0)
+    out = [sc.view(*spec) for spec in specs]
+    sc.close()
+    return out
+
+
 def bad_pixel_rate(depth: np.ndarray, gt: np.ndarray, rel: float = 0.01) -> float:
     """Share of pixels with |d - d_gt| / d_gt > rel."""
     valid = gt > 0
