@@ -474,16 +474,25 @@ def learned_vs_plain(sv, wl, device, flush, reps):
     out = {}
     runs = [("plain_20_sweeps", dict()),
             ("learned_4_sweeps", dict(init_mode=INIT_PROPOSAL, num_sweeps=4, perturbation=0.05)),
-            ("learned_8_sweeps", dict(init_mode=INIT_PROPOSAL, num_sweeps=8, perturbation=0.05))]
+            ("learned_8_sweeps", dict(init_mode=INIT_PROPOSAL, num_sweeps=8, perturbation=0.05)),
+            # the refinement step after the last sweep (the reference's never-launched kernel's
+            # 10 trials of sigma 0.05, and a finer 16 x 0.02)
+            ("plain_20_sweeps_refine_10x0.05", dict(refine_trials=10, refine_sigma=0.05)),
+            ("learned_4_sweeps_refine_10x0.05", dict(init_mode=INIT_PROPOSAL, num_sweeps=4, perturbation=0.05,
+                                                     refine_trials=10, refine_sigma=0.05)),
+            ("learned_4_sweeps_refine_16x0.02", dict(init_mode=INIT_PROPOSAL, num_sweeps=4, perturbation=0.05,
+                                                     refine_trials=16, refine_sigma=0.02))]
     params = proposal.load_params()
     net_ms = gflop = None
     for name, over in runs:
         e = Engine(sv.images, sv.ref_id, wl.params(gpu_id=device, **over))
-        net = proposal.for_engine(e, params) if over else None
+        learned = over.get("init_mode") == INIT_PROPOSAL
+        net = proposal.for_engine(e, params) if learned else None
         ms = _timed_runs(e, flush, reps)
         out[name] = {"ms_per_depth_map": round(ms, 3),
                      "bad_pixel_pct_1pct": round(100 * scene.bad_pixel_rate(e.depth(), sv.gt_depth), 3),
-                     "sweeps": 4 * wl.iterations if not over else over["num_sweeps"],
+                     "sweeps": over.get("num_sweeps", 4 * wl.iterations),
+                     "refine": [over["refine_trials"], over["refine_sigma"]] if "refine_trials" in over else None,
                      "cost_evals": e.stats().cost_evals}
         if net is not None and net_ms is None:
             # the network alone: forward of the 17-channel plane-sweep input
@@ -515,6 +524,53 @@ def learned_vs_plain(sv, wl, device, flush, reps):
                               "peak_tflops": peak, "frac_of_bf16_peak": round(tflops / peak, 5),
                               "peak_source": "MEASURED_PEAKS.json bf16_tflops (cuBLAS burst)"}
     return out
+
+
+def measure_fusion(engines, refs, warmup: int, reps: int) -> dict:
+    """Consistency filtering + fusion over the batch's depth maps, read in place (pm_fusion):
+    device time of the three kernels by CUDA events, the HBM roofline of the algorithmic bytes
+    (per pixel: its depth read once, fused depth and count written, 4 + 4 + 1 bytes; per kept
+    pixel: fused depth read again and a 16-byte point written) and what the filter keeps."""
+    from patchmatch_cuda_gb300 import Fusion, default_fuse_params, scene
+    fus = Fusion(engines)
+    params = default_fuse_params()
+    for _ in range(warmup):
+        fus.run(params)
+    check, total = [], []
+    for _ in range(reps):
+        fus.run(params)
+        inf = fus.info()
+        check.append(inf["ms_check"])
+        total.append(inf["ms_total"])
+    launches = fus.info()["launches"]
+    n_pts = fus.info()["points"]
+    pix = sum(e.width * e.height for e in engines)
+    checks = pix * (len(engines) - 1)
+    kept_bad, kept_share, raw_bad = [], [], []
+    for i, (e, sv) in enumerate(zip(engines, refs)):
+        f, _ = fus.depth(i)
+        gt = sv.gt_depth
+        valid = gt > 0
+        k = (f > 0) & valid
+        kept_share.append(float(k.sum() / max(valid.sum(), 1)))
+        kept_bad.append(float(np.mean(np.abs(f[k] - gt[k]) / gt[k] > 0.01)) if k.any() else 0.0)
+        raw_bad.append(scene.bad_pixel_rate(e.depth(), gt))
+    fus.close()
+    ms_total = float(np.median(total))
+    algo_bytes = pix * 9 + n_pts * 20
+    peaks = measured_peaks()
+    hbm = peaks.get("hbm_gbs")
+    achieved = algo_bytes / (ms_total * 1e-3) / 1e9
+    return {"params": {"max_reproj_px": params.max_reproj_px, "max_rel_depth": round(params.max_rel_depth, 6),
+                       "min_consistent": params.min_consistent},
+            "ms_check": round(float(np.median(check)), 4), "ms_total": round(ms_total, 4), "launches": launches,
+            "pixel_checks_per_s_G": round(checks / (float(np.median(check)) * 1e-3) / 1e9, 2),
+            "points": int(n_pts), "kept_share": round(float(np.mean(kept_share)), 4),
+            "bad_pixel_pct_1pct_kept": round(100 * float(np.mean(kept_bad)), 3),
+            "bad_pixel_pct_1pct_raw": round(100 * float(np.mean(raw_bad)), 3),
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                         "frac": round(achieved / hbm, 4) if hbm else None, "traffic": None,
+                         "algorithmic_bytes": int(algo_bytes)}}
 
 
 def run_batched(args):
@@ -558,6 +614,7 @@ def run_batched(args):
     barrier(world)
     total_ms, total_evals = allreduce_max_sum(world, sum(ms), float(evals * args.steps))
     bad = [scene.bad_pixel_rate(e.depth(), sv.gt_depth) for e, sv in zip(engines, refs)]
+    fusion = measure_fusion(engines, refs, max(args.warmup, 3), max(args.steps, 5))
     if rank == 0:
         print(json.dumps({
             "metric": "G cost-evals/s", "value": total_evals / (total_ms * 1e-3) / 1e9, "unit": "G cost-evals/s",
@@ -572,7 +629,7 @@ def run_batched(args):
                        "ms_per_batch": total_ms / args.steps, "mean_bad_pixel_pct_1pct": round(100 * float(np.mean(bad)), 3),
                        "texels": "u8 (the 8-bit inputs; half the bytes of FP16)",
                        "schedule": "one CUDA graph per batch; one launch per sweep over all references of a group",
-                       "warps_per_line": info["warps_per_line"]},
+                       "warps_per_line": info["warps_per_line"], "fusion": fusion},
             "gpu_launches": info["launches"] * args.steps, "clocks": clocks.summary(),
         }), flush=True)
     batch.close()

@@ -131,7 +131,16 @@ typedef struct pm_params {
                                       word) instead draw within +-perturbation x 2^(-k/4)
                                       (relative) of their current depth in sweep k, a local
                                       search that refines a learned initialisation         */
+    int refine_trials;             /* 0 (default): no refinement, as the reference runs
+                                      (patchMatch.cu:396). > 0: after the last sweep, that
+                                      many hypotheses depth + refine_sigma z (z ~ N(0, 1) by
+                                      Irwin-Hall) scored on the last sweep's sampled views;
+                                      the reference's never-launched depthRefinement
+                                      (patchMatch.cu:717-773) with 10 trials, sigma 0.05      */
+    float refine_sigma;            /* depth units (default 0.05)                              */
 } pm_params;
+
+#define PM_MAX_REFINE_TRIALS 256
 
 typedef struct pm_handle pm_handle;
 
@@ -201,6 +210,11 @@ pm_status pm_init_depth(pm_handle *h);
 pm_status pm_compute_costs(pm_handle *h, int axis);
 /* One sweep, topToDown / downToTop (patchMatch.cu:818-1209). sweep_id keys the random
  * draws; record_views writes the view-selection map. */
+/* Depth refinement (the step after the last sweep, see refine_trials): `trials` hypotheses
+ * around each pixel's depth on the views of rows 0 .. num_samples-1 of the view-selection map
+ * (0: all of pm_params.num_samples), window axis 0 (vertical sweeps) or 1 (horizontal),
+ * Philox draws keyed by sweep_id. Costs are left as they were. */
+pm_status pm_refine(pm_handle *h, int trials, float sigma, uint32_t sweep_id, int num_samples, int axis);
 pm_status pm_run_sweep(pm_handle *h, int direction, uint32_t sweep_id, int num_samples,
                        int record_views);
 pm_status pm_set_depth(pm_handle *h, const float *src);
@@ -369,7 +383,8 @@ pm_status pm_fusion_create_from_engines(pm_handle *const *hs, int n, pm_fusion *
 /* Filters and fuses; synchronous. May run again (e.g. after the engines ran again). */
 pm_status pm_fusion_run(pm_fusion *f, const pm_fuse_params *p);
 /* Points of the last run, the device time of the consistency kernel and of the whole fusion
- * (CUDA events, ms), and the kernels one run launches. */
+ * (CUDA events, ms), and the kernels one run launches (4: consistency, two scan passes,
+ * points). */
 pm_status pm_fusion_info(const pm_fusion *f, int64_t *num_points, float *ms_check, float *ms_total,
                          int *launches);
 /* Up to capacity points as (x, y, z, intensity in [0, 1]), reference by reference in row-major

@@ -8,13 +8,15 @@ patchMatch.cu:263-407, main.cpp:124-128), so this oracle pins the engine's own s
     back-projections R_i^T K_i^-1, -R_i^T t_i in float64 from the float32 cameras;
   * fuse(depths, pairs, bp, ...): the per-pixel round trip, counts, fused depths and points in
     float32, every operation rounded to nearest in the kernel's order (numpy's float32
-    elementwise arithmetic does not contract), so the same float32 matrices give the same bits.
+    elementwise arithmetic does not contract; 1 / z is correctly rounded as the kernel's
+    reciprocal is on (1e-30, 1e30)), so the same float32 matrices give the same bits.
 """
 from __future__ import annotations
 
 import numpy as np
 
 F = np.float32
+RCP_MIN, RCP_MAX = F(1e-30), F(1e30)
 
 
 def geometry(cams):
@@ -70,9 +72,10 @@ def fuse(depths, pairs, bp, max_reproj_px=1.0, max_rel_depth=0.01, min_consisten
                 Dj = np.asarray(depths[j], np.float32)
                 Hj, Wj = Dj.shape
                 pz = _apply(A, 2, u, v, d)
-                ok = valid & (pz > 0)
-                uj = _apply(A, 0, u, v, d) / pz
-                vj = _apply(A, 1, u, v, d) / pz
+                ok = valid & (pz > RCP_MIN) & (pz < RCP_MAX)
+                rz = F(1) / pz                      # the kernel's correctly rounded reciprocal
+                uj = _apply(A, 0, u, v, d) * rz
+                vj = _apply(A, 1, u, v, d) * rz
                 ok &= (uj >= 0) & (uj < F(Wj)) & (vj >= 0) & (vj < F(Hj))
                 ix = np.minimum(np.where(ok, uj, 0).astype(np.int64), Wj - 1)
                 iy = np.minimum(np.where(ok, vj, 0).astype(np.int64), Hj - 1)
@@ -82,10 +85,10 @@ def fuse(depths, pairs, bp, max_reproj_px=1.0, max_rel_depth=0.01, min_consisten
                 vc = iy.astype(np.float32) + F(0.5)
                 qz = _apply(B, 2, uc, vc, dj)
                 ok &= qz > 0
-                du = _apply(B, 0, uc, vc, dj) / qz - u
-                dv = _apply(B, 1, uc, vc, dj) / qz - v
-                err2 = du * du + dv * dv
-                ok &= (err2 < max_err2) & (np.abs(qz - d) < tol)
+                ex = _apply(B, 0, uc, vc, dj) - u * qz
+                ey = _apply(B, 1, uc, vc, dj) - v * qz
+                err2 = ex * ex + ey * ey
+                ok &= (err2 < max_err2 * (qz * qz)) & (np.abs(qz - d) < tol)
                 count += ok
                 acc = np.where(ok, acc + qz, acc)
             fused = np.zeros((H, W), np.float32)

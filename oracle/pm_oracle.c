@@ -448,6 +448,57 @@ void pmo_ncc_batch(const pmo_problem *p, const double *sum_i, const double *sum_
         out[i] = pmo_ncc(p, sum_i, sum_ii, xs[i], ys[i], views[i], depths[i], axes[i]);
 }
 
+long long pmo_refine(const pmo_problem *p, const double *sum_i, const double *sum_ii, double *depth,
+                     const unsigned char *view_sel, int num_samples, int trials, float sigma,
+                     uint32_t sweep_id, int axis)
+{
+    const int W = p->width, H = p->height, V = p->n_src;
+    const int npix = W * H;
+    const float d_lo = (float)p->depth_near;
+    const float d_hi = f_add(d_lo, (float)((double)(float)p->depth_far - (double)d_lo));
+    const float sqrt3 = (float)1.7320508075688772;
+    long long evals = 0;
+    #pragma omp parallel for schedule(dynamic, 64) reduction(+ : evals)
+    for (int pix = 0; pix < npix; ++pix) {
+        const int x = pix % W, y = pix / W;
+        int views[32], nv = 0;
+        for (int k = 0; k < num_samples && k < 32; ++k) {
+            const int v = view_sel[(size_t)k * npix + pix];
+            if (v < V) views[nv++] = v;
+        }
+        if (nv == 0) continue;
+        const real scale = plane_scale(p, x);
+        const float d0 = (float)depth[pix];
+        real best_cost = 0;
+        for (int k = 0; k < nv; ++k) best_cost += ncc_eval(p, sum_i, sum_ii, x, y, views[k], (real)d0, axis, scale);
+        best_cost /= (real)nv;
+        evals += nv;
+        float best = d0;
+        for (int t = 0; t < trials; ++t) {
+            const uint32_t ctr[4] = {(uint32_t)pix, sweep_id, ((uint32_t)PMO_RNG_REFINE << 16) | (uint32_t)t,
+                                     p->batch_id};
+            const uint32_t key[2] = {(uint32_t)p->seed, (uint32_t)(p->seed >> 32)};
+            uint32_t o[4];
+            pmo_philox4x32_10(ctr, key, o);
+            float u[4];
+            for (int k = 0; k < 4; ++k) u[k] = (float)((o[k] >> 8) + 1u) * (1.0f / 16777216.0f);
+            const float z = f_add(f_add(f_add(u[0], u[1]), f_add(u[2], u[3])), -2.0f);
+            const float dn = f_add(d0, f_mul(f_mul(z, sqrt3), sigma));
+            if (!(dn >= d_lo && dn <= d_hi)) continue;
+            real c = 0;
+            for (int k = 0; k < nv; ++k) c += ncc_eval(p, sum_i, sum_ii, x, y, views[k], (real)dn, axis, scale);
+            c /= (real)nv;
+            evals += nv;
+            if (c < best_cost) {
+                best_cost = c;
+                best = dn;
+            }
+        }
+        depth[pix] = (double)best;
+    }
+    return evals;
+}
+
 /* ------------------------------------------------------------------------------------
  * HMM view-selection messages, computeMessageBackward / computeMessageForward
  * (patchMatch.cu:669-715). A cost of exactly 2 (window outside the source) is replaced

@@ -39,7 +39,9 @@ enum {
     PMO_RNG_FWD_PRE = 3,   /* same, forward message with the old costs (:905)           */
     PMO_RNG_FWD_POST = 4,  /* same, forward message with the new costs (:874, :999)     */
     PMO_RNG_RAND_DEPTH = 5,/* random depth hypothesis (:937)                           */
-    PMO_RNG_SAMPLE = 6     /* view sample j (:942)                                      */
+    PMO_RNG_SAMPLE = 6,    /* view sample j (:942)                                      */
+    PMO_RNG_REFINE = 7     /* refinement trial (the engine's; the reference never runs
+                              its depthRefinement kernel, :717-773)                    */
 };
 
 typedef struct pmo_problem {
@@ -96,6 +98,15 @@ long long pmo_initial_costs(const pmo_problem *p, const double *sum_i, const dou
 long long pmo_sweep(const pmo_problem *p, const double *sum_i, const double *sum_ii,
                     double *depth, double *cost, int dir, uint32_t sweep_id, int num_samples,
                     unsigned char *view_sel, int line_begin, int line_end);
+/* Depth refinement as the engine's refine_kernel: per pixel, trials hypotheses d0 + sigma z
+ * (z = sqrt(3) (u1 + u2 + u3 + u4 - 2) in float from one Philox counter keyed (pixel, sweep_id,
+ * PMO_RNG_REFINE << 16 | trial, batch_id)), hypotheses outside [near, far] skipped, each scored
+ * by the mean cost over the views in rows 0 .. num_samples-1 of view_sel (entries >= n_src:
+ * none); the lowest mean below the current depth's replaces it. In place on depth; returns
+ * the evaluation count. */
+long long pmo_refine(const pmo_problem *p, const double *sum_i, const double *sum_ii, double *depth,
+                     const unsigned char *view_sel, int num_samples, int trials, float sigma,
+                     uint32_t sweep_id, int axis);
 long long pmo_run(const pmo_problem *p, int iterations, int num_samples,
                   const double *sum_i, const double *sum_ii,
                   double *depth, double *cost, unsigned char *view_sel);

@@ -60,6 +60,8 @@ def load(fp32: bool = False) -> C.CDLL:
     lib.pmo_ncc.argtypes = [P, P, P, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int]
     lib.pmo_ncc_batch.argtypes = [P, P, P, C.c_int, P, P, P, P, P, P]
     lib.pmo_init_depth.argtypes = [P, P]
+    lib.pmo_refine.restype = C.c_longlong
+    lib.pmo_refine.argtypes = [P, P, P, P, P, C.c_int, C.c_int, C.c_float, C.c_uint32, C.c_int]
     lib.pmo_initial_costs.restype = C.c_longlong
     lib.pmo_initial_costs.argtypes = [P, P, P, P, P]
     lib.pmo_sweep.restype = C.c_longlong
@@ -213,6 +215,14 @@ class Oracle:
         vs = view_sel.ctypes.data if view_sel is not None else None
         return self.lib.pmo_sweep(self._pp, self.sum_i.ctypes.data, self.sum_ii.ctypes.data, depth.ctypes.data,
                                   cost.ctypes.data, direction, sweep_id, num_samples, vs, lines[0], lines[1])
+
+    def refine(self, depth: np.ndarray, view_sel: np.ndarray, num_samples: int, trials: int, sigma: float,
+               sweep_id: int, axis: int) -> int:
+        """In-place on float64 depth (H, W) from a uint8 view-selection map (S, H, W)."""
+        assert depth.dtype == np.float64 and depth.flags.c_contiguous
+        vs = np.ascontiguousarray(view_sel, np.uint8)
+        return self.lib.pmo_refine(self._pp, self.sum_i.ctypes.data, self.sum_ii.ctypes.data, depth.ctypes.data,
+                                   vs.ctypes.data, num_samples, trials, sigma, sweep_id, axis)
 
     def run(self, iterations: int, num_samples: int):
         depth = np.empty((self.H, self.W), np.float64)

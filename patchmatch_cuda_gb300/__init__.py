@@ -309,6 +309,11 @@ class Engine:
     def run_sweep(self, direction: int, sweep_id: int, num_samples: int = 0, record_views: bool = False) -> None:
         self._chk(self._lib.pm_run_sweep(self.h, direction, sweep_id, num_samples, int(record_views)))
 
+    def refine(self, trials: int = 10, sigma: float = 0.05, sweep_id: int = 0, num_samples: int = 0,
+               axis: int = 0) -> None:
+        """pm_refine: depth refinement on the view-selection map's sampled views."""
+        self._chk(self._lib.pm_refine(self.h, trials, sigma, sweep_id, num_samples, axis))
+
     def set_depth(self, depth: np.ndarray) -> None:
         d = np.ascontiguousarray(depth, np.float32)
         assert d.shape == (self.height, self.width)

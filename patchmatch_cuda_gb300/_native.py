@@ -41,7 +41,7 @@ EXPORTED_SYMBOLS = [
     "pm_batch_run", "pm_batch_info", "pm_batch_destroy", "pm_texture_peak", "pm_default_fuse_params",
     "pm_fusion_create", "pm_fusion_create_from_engines", "pm_fusion_run", "pm_fusion_info",
     "pm_fusion_get_points", "pm_fusion_get_depth", "pm_fusion_geometry", "pm_fusion_write_ply",
-    "pm_fusion_last_error", "pm_fusion_destroy",
+    "pm_fusion_last_error", "pm_fusion_destroy", "pm_refine",
 ]
 
 MAX_FUSE_REFS = 256
@@ -63,7 +63,8 @@ class PmParams(C.Structure):
         ("init_mode", C.c_int), ("threads_per_line", C.c_int), ("quirks", C.c_int),
         ("gpu_id", C.c_int), ("block_dim_x", C.c_int), ("block_dim_y", C.c_int),
         ("sampler", C.c_int), ("texel_format", C.c_int), ("num_sweeps", C.c_int),
-        ("proposal_threshold", C.c_float), ("perturbation", C.c_float),
+        ("proposal_threshold", C.c_float), ("perturbation", C.c_float), ("refine_trials", C.c_int),
+        ("refine_sigma", C.c_float),
     ]
 
 
@@ -124,6 +125,7 @@ def load_engine() -> C.CDLL:
         "pm_init_depth": (C.c_int, [H]),
         "pm_compute_costs": (C.c_int, [H, C.c_int]),
         "pm_run_sweep": (C.c_int, [H, C.c_int, C.c_uint32, C.c_int, C.c_int]),
+        "pm_refine": (C.c_int, [H, C.c_int, C.c_float, C.c_uint32, C.c_int, C.c_int]),
         "pm_set_depth": (C.c_int, [H, P]),
         "pm_get_costs": (C.c_int, [H, P]),
         "pm_set_costs": (C.c_int, [H, P]),

@@ -236,6 +236,41 @@ cudaError_t enqueue_costs(pm_handle *h, int axis)
     return launch_window(window_side(h), h->p.sampler == PM_SAMPLER_HARDWARE, req);
 }
 
+// Window axis of a sweep direction: 1 for the horizontal sweeps (transposed windows).
+inline int orient(int dir) { return (dir == PM_DIR_LEFT_TO_RIGHT || dir == PM_DIR_RIGHT_TO_LEFT) ? 1 : 0; }
+
+// Depth refinement of descriptor `ref` of `refs` on stream s (refine_kernel).
+cudaError_t enqueue_refine(const pm_handle *h, const RefDesc *refs, int ref, int axis, int trials, float sigma,
+                           uint32_t sweep_id, int samples, cudaStream_t s)
+{
+    LaunchReq req{};
+    req.kind = LaunchKind::Refine;
+    req.stream = s;
+    req.refs = refs;
+    req.ref_index = ref;
+    req.axis = axis;
+    req.trials = trials;
+    req.sigma = sigma;
+    req.sweep_id = sweep_id;
+    req.samples = samples;
+    const int npix = h->W * h->H;
+    req.grid = (npix + COST_BLOCK / 32 - 1) / (COST_BLOCK / 32);
+    return launch_window(window_side(h), h->p.sampler == PM_SAMPLER_HARDWARE, req);
+}
+
+// The refinement that ends a schedule of `nsweeps` sweeps: on the last sweep's orientation and
+// sampled views (one sample when that sweep is in the first iteration after a random
+// initialisation), keyed by sweep id nsweeps.
+cudaError_t enqueue_final_refine(const pm_handle *h, const RefDesc *refs, int ref, int nsweeps, bool one_sample_first,
+                                 cudaStream_t s)
+{
+    if (h->p.refine_trials <= 0 || nsweeps <= 0) return cudaSuccess;
+    const int k = nsweeps - 1;
+    const int samples = (k / 4 == 0 && one_sample_first) ? 1 : h->p.num_samples;
+    return enqueue_refine(h, refs, ref, orient(k % 4), h->p.refine_trials, h->p.refine_sigma, (uint32_t)nsweeps,
+                          samples, s);
+}
+
 void fill_sweep_args(SweepArgs &a, const RefDesc *refs, const int *lines, int nrefs, int dir,
                      uint32_t sweep_id, int num_samples, int record)
 {
@@ -263,7 +298,6 @@ cudaError_t enqueue_sweep(int win, bool hw, int wpl, const SweepArgs &a, cudaStr
     return launch_window(win, hw, req);
 }
 
-inline int orient(int dir) { return (dir == PM_DIR_LEFT_TO_RIGHT || dir == PM_DIR_RIGHT_TO_LEFT) ? 1 : 0; }
 
 // ---- warps-per-line tuner ----------------------------------------------------------------
 // A line's steps are sequential, so a sweep takes ceil(lines / resident lines) line-times;
@@ -349,7 +383,7 @@ cudaError_t enqueue_schedule(pm_handle *h)
         e = enqueue_sweep(window_side(h), hw_of(h), h->wpl[orient(d)], a, h->stream);
         if (e != cudaSuccess) return e;
     }
-    return cudaSuccess;
+    return enqueue_final_refine(h, h->d_desc, 0, nsweeps, h->p.init_mode == PM_INIT_RANDOM, h->stream);
 }
 
 // Picks warps per line for both sweep orientations: the caller's choice, a remembered
@@ -446,6 +480,8 @@ void pm_default_params(pm_params *p)
     p->num_sweeps = 0;
     p->proposal_threshold = 0.5f;
     p->perturbation = 0.0f;
+    p->refine_trials = 0;
+    p->refine_sigma = 0.05f;
     p->threads_per_line = 0;
     p->quirks = 1;
     p->sampler = PM_SAMPLER_HARDWARE;
@@ -511,6 +547,8 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
         (p.init_mode != PM_INIT_RANDOM && p.init_mode != PM_INIT_PROPOSAL) || p.num_sweeps < 0 ||
         !(p.proposal_threshold >= 0.0f && p.proposal_threshold <= 1.0f) ||
         !(p.perturbation >= 0.0f && p.perturbation < 1.0f) ||
+        p.refine_trials < 0 || p.refine_trials > PM_MAX_REFINE_TRIALS ||
+        (p.refine_trials > 0 && !(p.refine_sigma > 0.0f && std::isfinite(p.refine_sigma))) ||
         (p.sampler != PM_SAMPLER_EXACT && p.sampler != PM_SAMPLER_HARDWARE) ||
         (p.texel_format != PM_TEXELS_AUTO && p.texel_format != PM_TEXELS_U8 &&
          p.texel_format != PM_TEXELS_F16 && p.texel_format != PM_TEXELS_F32) ||
@@ -793,6 +831,7 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
     D.ik00 = (float)kr_inv[0];
     D.ik02 = (float)kr_inv[2];
     D.quirks = p.quirks ? 1 : 0;
+    D.record_sweep = -1;
     D.hw_filter = h->p.sampler == PM_SAMPLER_HARDWARE ? 1 : 0;
     D.batch_id = 0;
     D.seed = p.seed;
@@ -939,6 +978,14 @@ cudaError_t enqueue_batch(pm_batch *b, cudaStream_t s)
             if (e != cudaSuccess) return e;
             ++b->launches;
         }
+        for (int i = 0; i < m; ++i) {
+            pm_handle *h = g.refs[i];
+            if (h->p.refine_trials <= 0) continue;
+            const cudaError_t e = enqueue_final_refine(h, g.d_descs, i, schedule_sweeps(h),
+                                                       g.refs[0]->p.init_mode == PM_INIT_RANDOM, s);
+            if (e != cudaSuccess) return e;
+            ++b->launches;
+        }
     }
     return cudaGetLastError();
 }
@@ -1020,8 +1067,12 @@ pm_status batch_setup(pm_handle *const *hs, int n, pm_batch *b)
             g.win = grp[0]->win;
             g.hw = hw_of(grp[0]);
             PM_CUDA(hs[0], cudaMalloc((void **)&g.d_descs, sizeof(RefDesc) * g.refs.size()));
-            for (size_t i = 0; i < g.refs.size(); ++i)
-                PM_CUDA(hs[0], cudaMemcpy(g.d_descs + i, &g.refs[i]->h_desc, sizeof(RefDesc), cudaMemcpyHostToDevice));
+            for (size_t i = 0; i < g.refs.size(); ++i) {
+                // each reference records the views of its own last sweep only, as a single run does
+                RefDesc d = g.refs[i]->h_desc;
+                d.record_sweep = schedule_sweeps(g.refs[i]) - 1;
+                PM_CUDA(hs[0], cudaMemcpy(g.d_descs + i, &d, sizeof(RefDesc), cudaMemcpyHostToDevice));
+            }
             b->groups.push_back(g);
         }
     }
@@ -1225,6 +1276,19 @@ pm_status pm_compute_costs(pm_handle *h, int axis)
     pm_status st = set_device(h);
     if (st != PM_OK) return st;
     PM_CUDA(h, enqueue_costs(h, axis));
+    PM_CUDA(h, cudaStreamSynchronize(h->stream));
+    return PM_OK;
+}
+
+pm_status pm_refine(pm_handle *h, int trials, float sigma, uint32_t sweep_id, int num_samples, int axis)
+{
+    if (!h || trials < 0 || trials > PM_MAX_REFINE_TRIALS || !(sigma > 0.0f && std::isfinite(sigma)) ||
+        num_samples < 0 || num_samples > h->p.num_samples || (axis != 0 && axis != 1))
+        return PM_ERR_INVALID_ARGUMENT;
+    if (!h->has_depth) return fail(h, PM_ERR_STATE, "pm_refine needs a depth map");
+    pm_status st = set_device(h);
+    if (st != PM_OK) return st;
+    PM_CUDA(h, enqueue_refine(h, h->d_desc, 0, axis, trials, sigma, sweep_id, num_samples, h->stream));
     PM_CUDA(h, cudaStreamSynchronize(h->stream));
     return PM_OK;
 }

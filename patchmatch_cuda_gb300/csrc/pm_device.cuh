@@ -21,7 +21,7 @@ constexpr int MAX_VIEWS = 32;
 // Random-draw purposes; a draw is keyed by (pixel, sweep, purpose << 16 | sub, batch).
 enum : uint32_t {
     RNG_INIT = 1, RNG_BWD = 2, RNG_FWD_PRE = 3, RNG_FWD_POST = 4, RNG_RAND_DEPTH = 5,
-    RNG_SAMPLE = 6
+    RNG_SAMPLE = 6, RNG_REFINE = 7
 };
 constexpr uint32_t INIT_SWEEP_ID = 0xFFFFFFFFu;
 
@@ -40,6 +40,9 @@ struct RefDesc {
     float nx, nz, ik00, ik02;       // plane scale s = nx (ik00 (x+1/2) + ik02) + nz
     int quirks;
     int hw_filter;                  // textures filter bilinearly in hardware
+    int record_sweep;               // >= 0: views are recorded only in this sweep (batches,
+                                    // whose launches record for all references); -1: whenever
+                                    // the launch records
     uint32_t batch_id;
     uint64_t seed;
     const float *ref;               // height*width texels
@@ -88,6 +91,17 @@ __device__ __forceinline__ float2 draw_uniform2(uint64_t seed, uint32_t pixel, u
                                   make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)));
     return make_float2((float)((o.x >> 8) + 1u) * (1.0f / 16777216.0f),
                        (float)((o.y >> 8) + 1u) * (1.0f / 16777216.0f));
+}
+
+// All four words of the counter as uniforms in (0, 1].
+__device__ __forceinline__ float4 draw_uniform4(uint64_t seed, uint32_t pixel, uint32_t sweep,
+                                                uint32_t purpose, uint32_t sub, uint32_t batch)
+{
+    const uint4 o = philox4x32_10(make_uint4(pixel, sweep, (purpose << 16) | sub, batch),
+                                  make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)));
+    constexpr float k = 1.0f / 16777216.0f;
+    return make_float4((float)((o.x >> 8) + 1u) * k, (float)((o.y >> 8) + 1u) * k,
+                       (float)((o.z >> 8) + 1u) * k, (float)((o.w >> 8) + 1u) * k);
 }
 
 // ---- source fetch --------------------------------------------------------------------------

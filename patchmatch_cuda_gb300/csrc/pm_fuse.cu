@@ -13,8 +13,9 @@
 // reference in row-major order.
 //
 // The per-pixel arithmetic is FP32 with explicit round-to-nearest operations (no contraction)
-// in a fixed order, so a CPU restatement in the same order gives the same bits from the same
-// FP32 matrices (pm_fusion_geometry).
+// in a fixed order and a correctly rounded reciprocal, so a CPU restatement in the same order
+// gives the same bits from the same FP32 matrices (pm_fusion_geometry). The round trip's
+// reprojection test is division-free: |q - qz (u, v)|^2 < max_reproj_px^2 qz^2.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -33,6 +34,11 @@ namespace pm {
 namespace {
 
 constexpr int FUSE_THREADS = 256;
+// Projection depths outside this range are rejected, so that rcp_nr (correct rounding for a
+// normal argument with a normal reciprocal) equals 1 / z exactly.
+constexpr float RCP_MIN = 1e-30f, RCP_MAX = 1e30f;
+// Blocks per scan tile (one CTA of 1024 threads scans a tile).
+constexpr int SCAN_TILE_LOG2 = 10;
 
 struct FuseRefDev {
     const float *depth;       // width * height, row-major
@@ -57,7 +63,8 @@ __device__ __forceinline__ float apply_row(const float *m, int k, float u, float
 
 __global__ void __launch_bounds__(FUSE_THREADS)
 fuse_check_kernel(const FuseRefDev *__restrict__ refs, const float *__restrict__ pairs, int n,
-                  float max_err2, float max_rel, int min_consistent, uint32_t *__restrict__ block_kept)
+                  float max_err2, float max_rel, int min_consistent, uint32_t *__restrict__ block_kept,
+                  uint32_t *__restrict__ tile_kept)
 {
     __shared__ float s_fwd[PM_MAX_FUSE_REFS * 12];   // i -> j
     __shared__ float s_bwd[PM_MAX_FUSE_REFS * 12];   // j -> i
@@ -96,9 +103,10 @@ fuse_check_kernel(const FuseRefDev *__restrict__ refs, const float *__restrict__
                 if (j == i) continue;
                 const float *A = s_fwd + 12 * j;
                 const float pz = apply_row(A, 2, u, v, d);
-                if (!(pz > 0.0f)) continue;
-                const float uj = __fdiv_rn(apply_row(A, 0, u, v, d), pz);
-                const float vj = __fdiv_rn(apply_row(A, 1, u, v, d), pz);
+                if (!(pz > RCP_MIN && pz < RCP_MAX)) continue;
+                const float rz = rcp_nr(pz);   // correctly rounded in this range
+                const float uj = mul(apply_row(A, 0, u, v, d), rz);
+                const float vj = mul(apply_row(A, 1, u, v, d), rz);
                 const int2 sz = s_size[j];
                 if (!(uj >= 0.0f && uj < (float)sz.x && vj >= 0.0f && vj < (float)sz.y)) continue;
                 const int ix = min((int)uj, sz.x - 1), iy = min((int)vj, sz.y - 1);
@@ -108,10 +116,11 @@ fuse_check_kernel(const FuseRefDev *__restrict__ refs, const float *__restrict__
                 const float uc = add((float)ix, 0.5f), vc = add((float)iy, 0.5f);
                 const float qz = apply_row(B, 2, uc, vc, dj);
                 if (!(qz > 0.0f)) continue;
-                const float du = add(__fdiv_rn(apply_row(B, 0, uc, vc, dj), qz), -u);
-                const float dv = add(__fdiv_rn(apply_row(B, 1, uc, vc, dj), qz), -v);
-                const float err2 = add(mul(du, du), mul(dv, dv));
-                if (err2 < max_err2 && fabsf(add(qz, -d)) < tol) {
+                // |q / qz - (u, v)|^2 < max_err2 without dividing: |q - qz (u, v)|^2 < max_err2 qz^2
+                const float ex = add(apply_row(B, 0, uc, vc, dj), -mul(u, qz));
+                const float ey = add(apply_row(B, 1, uc, vc, dj), -mul(v, qz));
+                const float err2 = add(mul(ex, ex), mul(ey, ey));
+                if (err2 < mul(max_err2, mul(qz, qz)) && fabsf(add(qz, -d)) < tol) {
                     ++count;
                     acc = add(acc, qz);
                 }
@@ -127,49 +136,71 @@ fuse_check_kernel(const FuseRefDev *__restrict__ refs, const float *__restrict__
         R.count[pix] = (uint8_t)min(count, 255);
     }
     const int kept = __syncthreads_count(keep);
-    if (threadIdx.x == 0) block_kept[(size_t)i * gridDim.x + blockIdx.x] = (uint32_t)kept;
+    if (threadIdx.x == 0) {
+        const size_t blk = (size_t)i * gridDim.x + blockIdx.x;
+        block_kept[blk] = (uint32_t)kept;
+        if (kept) atomicAdd(tile_kept + (blk >> SCAN_TILE_LOG2), (uint32_t)kept);   // integer: order-free
+    }
 }
 
-// Exclusive prefix sum of the per-block counts (one CTA; few hundred thousand blocks at most)
-// and the total.
-__global__ void __launch_bounds__(1024)
-fuse_scan_kernel(const uint32_t *__restrict__ counts, int nblocks, unsigned long long *__restrict__ offsets,
-                 unsigned long long *__restrict__ total)
+// Exclusive scan of one value per thread over a CTA of 1024 threads; *total gets the sum.
+__device__ __forceinline__ unsigned long long cta_exclusive_scan(unsigned long long val, unsigned long long *s_warp,
+                                                                 unsigned long long *total)
 {
-    __shared__ unsigned long long s_warp[32];
-    __shared__ unsigned long long s_carry;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (threadIdx.x == 0) s_carry = 0;
+    unsigned long long inc = val;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += t;
+    }
+    if (lane == 31) s_warp[wid] = inc;
     __syncthreads();
-    for (int base = 0; base < nblocks; base += 1024) {
-        const int k = base + threadIdx.x;
-        const unsigned long long val = k < nblocks ? counts[k] : 0ull;
-        unsigned long long inc = val;
+    if (wid == 0) {
+        unsigned long long w = s_warp[lane];
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            const unsigned long long t = __shfl_up_sync(0xffffffffu, inc, o);
-            if (lane >= o) inc += t;
+            const unsigned long long t = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += t;
         }
-        if (lane == 31) s_warp[wid] = inc;
-        __syncthreads();
-        if (wid == 0) {
-            unsigned long long w = s_warp[lane];
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const unsigned long long t = __shfl_up_sync(0xffffffffu, w, o);
-                if (lane >= o) w += t;
-            }
-            s_warp[lane] = w;   // inclusive over warps
-        }
-        __syncthreads();
-        const unsigned long long warp_base = wid ? s_warp[wid - 1] : 0ull;
-        const unsigned long long carry = s_carry;
-        if (k < nblocks) offsets[k] = carry + warp_base + inc - val;
-        __syncthreads();
-        if (threadIdx.x == 0) s_carry = carry + s_warp[31];
-        __syncthreads();
+        s_warp[lane] = w;   // inclusive over warps
     }
-    if (threadIdx.x == 0) *total = s_carry;
+    __syncthreads();
+    const unsigned long long out = (wid ? s_warp[wid - 1] : 0ull) + inc - val;
+    *total = s_warp[31];
+    __syncthreads();        // s_warp may be reused by the caller
+    return out;
+}
+
+// Exclusive scan of the tiles' kept counts (at most a few thousand tiles) into tile_base, and
+// the total; one CTA.
+__global__ void __launch_bounds__(1024)
+fuse_scan_tiles_kernel(const uint32_t *__restrict__ tile_kept, int ntiles, unsigned long long *__restrict__ tile_base,
+                       unsigned long long *__restrict__ total)
+{
+    __shared__ unsigned long long s_warp[32];
+    unsigned long long carry = 0;
+    for (int base = 0; base < ntiles; base += 1024) {
+        const int k = base + threadIdx.x;
+        unsigned long long chunk;
+        const unsigned long long ex = cta_exclusive_scan(k < ntiles ? tile_kept[k] : 0ull, s_warp, &chunk);
+        if (k < ntiles) tile_base[k] = carry + ex;
+        carry += chunk;
+    }
+    if (threadIdx.x == 0) *total = carry;
+}
+
+// Offsets of the blocks of one tile (1024 blocks per CTA): the tile's base plus the exclusive
+// scan of its blocks' counts.
+__global__ void __launch_bounds__(1024)
+fuse_scan_blocks_kernel(const uint32_t *__restrict__ block_kept, int nblocks,
+                        const unsigned long long *__restrict__ tile_base, unsigned long long *__restrict__ offsets)
+{
+    __shared__ unsigned long long s_warp[32];
+    const int k = (blockIdx.x << SCAN_TILE_LOG2) + threadIdx.x;
+    unsigned long long chunk;
+    const unsigned long long ex = cta_exclusive_scan(k < nblocks ? block_kept[k] : 0ull, s_warp, &chunk);
+    if (k < nblocks) offsets[k] = tile_base[blockIdx.x] + ex;
 }
 
 // Writes the kept pixels' points (x, y, z, intensity) at their block's offset, in pixel order.
@@ -245,8 +276,9 @@ struct pm_fusion {
     std::vector<pm::FuseRefDev> h_refs;
     pm::FuseRefDev *d_refs = nullptr;
     float *d_pairs = nullptr;
-    uint32_t *d_block_kept = nullptr;
-    unsigned long long *d_offsets = nullptr, *d_total = nullptr, *h_total = nullptr;
+    uint32_t *d_block_kept = nullptr, *d_tile_kept = nullptr;
+    unsigned long long *d_offsets = nullptr, *d_tile_base = nullptr, *d_total = nullptr, *h_total = nullptr;
+    int ntiles = 0;
     float4 *d_points = nullptr;
     std::vector<void *> owned;      // device buffers this object allocated
     int max_blocks = 0;
@@ -421,6 +453,9 @@ pm_status fusion_create(const FuseSource *sources, int n, int device, pm_fusion 
     FUSE_TRY(fuse_alloc(f, &f->d_pairs, f->pairs.size() * 4));
     FUSE_TRY(fuse_alloc(f, &f->d_block_kept, nblk * 4));
     FUSE_TRY(fuse_alloc(f, &f->d_offsets, nblk * 8));
+    f->ntiles = (int)((nblk + (1u << pm::SCAN_TILE_LOG2) - 1) >> pm::SCAN_TILE_LOG2);
+    FUSE_TRY(fuse_alloc(f, &f->d_tile_kept, (size_t)f->ntiles * 4));
+    FUSE_TRY(fuse_alloc(f, &f->d_tile_base, (size_t)f->ntiles * 8));
     FUSE_TRY(fuse_alloc(f, &f->d_total, 8));
     FUSE_TRY(fuse_alloc(f, &f->d_points, (size_t)f->total_pix * sizeof(float4)));
     FUSE_TRY(cudaMemcpyAsync(f->d_refs, f->h_refs.data(), sizeof(FuseRefDev) * n, cudaMemcpyHostToDevice, f->stream));
@@ -478,14 +513,18 @@ pm_status pm_fusion_run(pm_fusion *f, const pm_fuse_params *p)
     const dim3 grid((unsigned)f->max_blocks, (unsigned)f->n);
     const int nblk = f->max_blocks * f->n;
     const float err2 = p->max_reproj_px * p->max_reproj_px;
+    FUSE_CUDA(f, cudaMemsetAsync(f->d_tile_kept, 0, (size_t)f->ntiles * 4, f->stream), "tile counts");
     FUSE_CUDA(f, cudaEventRecord(f->ev[0], f->stream), "event");
     pm::fuse_check_kernel<<<grid, pm::FUSE_THREADS, 0, f->stream>>>(f->d_refs, f->d_pairs, f->n, err2,
                                                                      p->max_rel_depth, p->min_consistent,
-                                                                     f->d_block_kept);
+                                                                     f->d_block_kept, f->d_tile_kept);
     FUSE_CUDA(f, cudaGetLastError(), "fuse_check_kernel");
     FUSE_CUDA(f, cudaEventRecord(f->ev[1], f->stream), "event");
-    pm::fuse_scan_kernel<<<1, 1024, 0, f->stream>>>(f->d_block_kept, nblk, f->d_offsets, f->d_total);
-    FUSE_CUDA(f, cudaGetLastError(), "fuse_scan_kernel");
+    pm::fuse_scan_tiles_kernel<<<1, 1024, 0, f->stream>>>(f->d_tile_kept, f->ntiles, f->d_tile_base, f->d_total);
+    FUSE_CUDA(f, cudaGetLastError(), "fuse_scan_tiles_kernel");
+    pm::fuse_scan_blocks_kernel<<<f->ntiles, 1024, 0, f->stream>>>(f->d_block_kept, nblk, f->d_tile_base,
+                                                                   f->d_offsets);
+    FUSE_CUDA(f, cudaGetLastError(), "fuse_scan_blocks_kernel");
     pm::fuse_points_kernel<<<grid, pm::FUSE_THREADS, 0, f->stream>>>(f->d_refs, f->d_offsets, f->d_points);
     FUSE_CUDA(f, cudaGetLastError(), "fuse_points_kernel");
     FUSE_CUDA(f, cudaEventRecord(f->ev[2], f->stream), "event");
@@ -505,7 +544,7 @@ pm_status pm_fusion_info(const pm_fusion *f, int64_t *num_points, float *ms_chec
     if (num_points) *num_points = f->n_points;
     if (ms_check) *ms_check = f->ms_check;
     if (ms_total) *ms_total = f->ms_total;
-    if (launches) *launches = 3;
+    if (launches) *launches = 4;
     return PM_OK;
 }
 

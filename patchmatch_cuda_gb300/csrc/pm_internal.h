@@ -9,7 +9,7 @@
 
 namespace pm {
 
-enum class LaunchKind { Sweep, Costs, Eval, SweepOccupancy };
+enum class LaunchKind { Sweep, Costs, Eval, SweepOccupancy, Refine };
 
 struct LaunchReq {
     LaunchKind kind;
@@ -27,6 +27,11 @@ struct LaunchReq {
     const int4 *queries;
     const float *depths;
     float *out;
+    // Refine (axis, refs, ref_index as Costs)
+    int trials;
+    float sigma;
+    uint32_t sweep_id;
+    int samples;
 };
 
 // Window-size and sampler dispatch, split over translation units so they compile in

@@ -7,6 +7,7 @@
 //  costs_kernel<W>  every view's cost at the current depth, computeAllCostGivenDepth
 //                   (patchMatch.cu:775-816); one warp per pixel, two views per pass.
 //  eval_kernel<W>   windowed NCC for arbitrary (x, y, view, depth, axis) queries.
+//  refine_kernel<W> depth refinement around the final depth on the last sweep's sampled views.
 #pragma once
 
 #include "pm_device.cuh"
@@ -386,7 +387,7 @@ __global__ void __maxnreg__(SweepRegs<HW>::value) sweep_kernel(const __grid_cons
                 n_alg += 2 * tested;
                 n_done += 2 * nu;
             }
-            if (A.record_views && lane < S)
+            if (A.record_views && lane < S && (D.record_sweep < 0 || (int)sweep == D.record_sweep))
                 D.view_sel[(size_t)lane * Wd * Hd + pix] = (uint8_t)(my_sel < 0 ? 255 : my_sel);
             // forward message from the previous step's with the new costs (:996-999)
             if (vl) {
@@ -473,6 +474,83 @@ __global__ void __launch_bounds__(COST_BLOCK) eval_kernel(const RefDesc *refs, i
         float v, unused;
         ncc_pair<W, HW>(D, s_hh, wc, tab, col, lane, t.z, depths[i], t.z, depths[i], v, unused);
         if (lane == 0) out[i] = v;
+    }
+}
+
+// Depth refinement after the last sweep, the step the reference leaves out (patchMatch.cu:396;
+// its never-launched depthRefinement kernel, :717-773): `trials` hypotheses d0 + sigma z around
+// the current depth d0, z approximately standard normal (Irwin-Hall: sqrt(3) (u1 + u2 + u3 + u4
+// - 2) from the four 24-bit uniforms of one Philox counter, in FP32 in this order), each scored
+// by the mean cost over the views the last sweep sampled for the pixel (view_sel rows 0 ..
+// samples-1, entries >= n_src meaning none); the lowest mean below the current depth's mean
+// replaces it. Hypotheses outside [near, far] are skipped. Where the reference's kernel
+// compares against one stored view cost and writes an uninitialised depth when no trial
+// improves, this one compares against the mean at the current depth and keeps that depth.
+// One warp per pixel.
+constexpr float REFINE_SQRT3 = 1.7320508075688772f;
+
+template <int W, bool HW>
+__global__ void __launch_bounds__(COST_BLOCK) refine_kernel(const RefDesc *refs, int r, int axis, int trials,
+                                                            float sigma, uint32_t sweep_id, int samples)
+{
+    constexpr int TAB = Window<W>::TAB;
+    __shared__ RefDesc D;
+    __shared__ float4 s_hh[5 * MAX_VIEWS];
+    stage_ref(refs[r], D, s_hh);
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int npix = D.width * D.height;
+    const int S = samples > 0 ? min(samples, D.num_samples) : D.num_samples;
+    __shared__ float tabs[COST_BLOCK / 32][TAB];
+    __shared__ float cols[COST_BLOCK / 32][W];
+    __shared__ WinCtl wcs[COST_BLOCK / 32];
+    float *tab = tabs[threadIdx.x >> 5];
+    float *col = cols[threadIdx.x >> 5];
+    WinCtl &wc = wcs[threadIdx.x >> 5];
+    const float d_lo = D.depth_near, d_hi = __fadd_rn(D.depth_near, D.depth_span);
+    unsigned long long evals = 0;
+    const int warps = (int)((gridDim.x * blockDim.x) >> 5);
+    for (int p = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); p < npix; p += warps) {
+        const int x = p % D.width, y = p / D.width;
+        const int my_view = (lane < S && D.view_sel) ? (int)D.view_sel[(size_t)lane * npix + p] : 255;
+        const unsigned mask = __ballot_sync(FULL_MASK, my_view < D.n_src);
+        if (!mask) continue;
+        const int nv = __popc(mask);
+        __syncwarp();
+        load_window<W>(D, x, y, axis, lane, tab, col, wc);
+        __syncwarp();
+        const float d0 = D.depth[p];
+        auto score = [&](float dd) {
+            float sum = 0.0f;
+            for (int t = 0; t < nv; t += 2) {
+                const int va = __shfl_sync(FULL_MASK, my_view, nth_bit(mask, t));
+                const int vb = t + 1 < nv ? __shfl_sync(FULL_MASK, my_view, nth_bit(mask, t + 1)) : va;
+                float na, nb;
+                ncc_pair<W, HW>(D, s_hh, wc, tab, col, lane, va, dd, vb, dd, na, nb);
+                sum = __fadd_rn(sum, na);
+                if (t + 1 < nv) sum = __fadd_rn(sum, nb);
+            }
+            return __fdiv_rn(sum, (float)nv);
+        };
+        float best = d0, best_cost = score(d0);
+        evals += (unsigned long long)nv;
+        for (int t = 0; t < trials; ++t) {
+            const float4 u = draw_uniform4(D.seed, (uint32_t)p, sweep_id, RNG_REFINE, (uint32_t)t, D.batch_id);
+            const float z = __fadd_rn(__fadd_rn(__fadd_rn(u.x, u.y), __fadd_rn(u.z, u.w)), -2.0f);
+            const float dn = __fadd_rn(d0, __fmul_rn(__fmul_rn(z, REFINE_SQRT3), sigma));
+            if (!(dn >= d_lo && dn <= d_hi)) continue;
+            const float c = score(dn);
+            evals += (unsigned long long)nv;
+            if (c < best_cost) {
+                best = dn;
+                best_cost = c;
+            }
+        }
+        if (lane == 0) D.depth[p] = best;
+    }
+    if (lane == 0 && evals) {
+        atomicAdd(D.evals, evals);
+        atomicAdd(D.evals + 1, evals);
     }
 }
 

@@ -67,6 +67,8 @@ def _create(views, ref_id, **over):
     (dict(num_samples=33), 1), (dict(depth_near=-1.0, depth_far=-1.0), 1), (dict(depth_far=0.5), 1),
     (dict(sp_alpha=0.0), 1), (dict(num_iterations=0), 1), (dict(prefilter=7), 1),
     (dict(prefilter=2, gaussian_sigma=0.0), 1), (dict(precision=5), 1),
+    (dict(refine_trials=-1), 1), (dict(refine_trials=257), 1), (dict(refine_trials=4, refine_sigma=0.0), 1),
+    (dict(refine_trials=4, refine_sigma=float("inf")), 1),
 ])
 def test_invalid_parameters_are_rejected(engine_lib, over, status):
     assert _create(_views(), 0, **over) == status
@@ -93,3 +95,32 @@ def test_status_strings(engine_lib):
     assert engine_lib.pm_status_string(0) == b"ok"
     assert engine_lib.pm_status_string(2) == b"window size out of range"
     assert engine_lib.pm_status_string(99) == b"unknown status"
+
+
+def test_fusion_arguments_are_checked_before_the_device(engine_lib):
+    """pm_fusion_create rejects bad counts, missing depth maps and cameras without a GPU."""
+    from patchmatch_cuda_gb300 import _native
+    lib = _native.load_engine()
+    d = np.ones((4, 5), np.float32)
+    views = (_native.PmDepthView * 2)()
+    for v in views:
+        v.depth, v.width, v.height = d.ctypes.data, 5, 4
+        v.K[:] = [5.0, 0, 2.5, 0, 5.0, 2.0, 0, 0, 1]
+        v.R[:] = [1.0, 0, 0, 0, 1, 0, 0, 0, 1]
+    h = C.c_void_p()
+    assert lib.pm_fusion_create(views, 0, -1, C.byref(h)) == 1
+    assert lib.pm_fusion_create(views, 257, -1, C.byref(h)) == 1
+    views[1].depth = None
+    assert lib.pm_fusion_create(views, 2, -1, C.byref(h)) == 5
+    views[1].depth = d.ctypes.data
+    views[1].width = 0
+    assert lib.pm_fusion_create(views, 2, -1, C.byref(h)) == 5
+    views[1].width = 5
+    views[1].t[0] = float("nan")
+    assert lib.pm_fusion_create(views, 2, -1, C.byref(h)) == 6
+    assert lib.pm_fusion_create_from_engines(None, 1, C.byref(h)) == 1
+    assert not h.value
+    p = _native.PmFuseParams()
+    lib.pm_default_fuse_params(C.byref(p))
+    assert (p.max_reproj_px, round(p.max_rel_depth, 6), p.min_consistent) == (1.0, 0.01, 2)
+

@@ -68,13 +68,14 @@ def test_batched_run_equals_single_runs(small):
     for sv in (small, sv2):
         e = _engine(sv)
         e.run()
-        singles.append((e.depth(), e.costs()))
+        singles.append((e.depth(), e.costs(), e.view_selection()))
         e.close()
     engines = [_engine(small), _engine(sv2)]
     run_batch(engines)
-    for e, (d, c) in zip(engines, singles):
+    for e, (d, c, vs) in zip(engines, singles):
         np.testing.assert_array_equal(e.depth(), d)
         np.testing.assert_array_equal(e.costs(), c)
+        np.testing.assert_array_equal(e.view_selection(), vs)     # each reference's last sweep
         e.close()
 
 
@@ -144,6 +145,48 @@ def test_cli_on_an_nvm_model_matches_the_library(small, tmp_path):
     eng.close()
     gt = small.gt_depth
     assert scene.bad_pixel_rate(d, gt, 0.05) < 0.5             # the NVM cameras reconstruct the scene
+
+
+def test_refinement_in_the_schedule(small):
+    """refine_trials > 0 appends the refinement to the run: the same as a plain run followed by
+    pm_refine on the last sweep's views (keyed by the sweep count), in singles and batches; a
+    depth changes only to one with a lower mean cost over the pixel's sampled views."""
+    from patchmatch_cuda_gb300 import Batch
+    w = small.workload
+    plain = _engine(small)
+    plain.run()
+    before = plain.depth()
+    plain.refine(10, 0.05, 4 * w.iterations, w.num_samples, 0)       # last sweep: bottom to top
+    want = plain.depth()
+    views = plain.view_selection()
+    eng = _engine(small, refine_trials=10, refine_sigma=0.05)
+    eng.run()
+    np.testing.assert_array_equal(eng.depth(), want)
+    b = Batch([eng])
+    b.run()
+    np.testing.assert_array_equal(eng.depth(), want)
+    np.testing.assert_array_equal(eng.view_selection(), views)    # the last sweep's, as a single run
+    b.close()
+    # where a depth changed, the mean cost over the pixel's sampled views fell (pm_eval_costs)
+    ys, xs = np.nonzero(want != before)
+    assert len(ys) > 0.02 * want.size
+    sel = np.random.default_rng(0).choice(len(ys), min(2000, len(ys)), replace=False)
+    qx, qy, qv, qd0, qd1, owner = [], [], [], [], [], []
+    for k in sel:
+        y, x = ys[k], xs[k]
+        for v in views[:, y, x]:
+            if v < plain.n_src:
+                qx.append(x); qy.append(y); qv.append(v); qd0.append(before[y, x]); qd1.append(want[y, x])
+                owner.append(k)
+    axes = np.zeros(len(qx), np.int32)
+    c0 = plain.eval_costs(qx, qy, qv, qd0, axes)
+    c1 = plain.eval_costs(qx, qy, qv, qd1, axes)
+    owner = np.array(owner)
+    for k in np.unique(owner):
+        m = owner == k
+        assert c1[m].mean() < c0[m].mean() + 1e-6
+    plain.close()
+    eng.close()
 
 
 def test_reference_mirror_class(small):

@@ -64,7 +64,7 @@ def test_fusion_matches_the_oracle_bit_for_bit(views, parity_log):
                    default_fuse_params(min_consistent=0), default_fuse_params(min_consistent=3, max_rel_depth=0.002)):
         _compare(fus, depths, grays, params, parity_log, f"fusion_min{params.min_consistent}")
     info = fus.info()
-    assert info["launches"] == 3 and info["ms_total"] >= info["ms_check"] > 0
+    assert info["launches"] == 4 and info["ms_total"] >= info["ms_check"] > 0
     fus.close()
 
 
@@ -164,3 +164,16 @@ def test_fusion_removes_wrong_depths(parity_log):
     fus.close()
     for e in engines:
         e.close()
+
+
+def test_fusion_over_several_scan_tiles(parity_log):
+    """Four 640x480 maps (4800 blocks of 256 pixels: five scan tiles of 1024 blocks), bit-exact."""
+    from patchmatch_cuda_gb300 import Fusion, default_fuse_params, scene
+    specs = [(yaw, 0.0, 640, 480, 600.0) for yaw in (-6.0, -2.0, 2.0, 6.0)]
+    vs = scene.scene_views(specs, seed=4, n_planes=6, n_boxes=20)
+    depths = _noisy(vs, seed=5)
+    images = [im for im, _ in vs]
+    fus = Fusion.from_depth_maps(depths, images)
+    n = _compare(fus, depths, [im.image for im in images], default_fuse_params(), parity_log, "fusion_640x480x4")
+    assert n > 100000
+    fus.close()

@@ -345,6 +345,32 @@ def test_sweep_lockstep_local_search(small_scene, direction, parity_log):
     eng.close()
 
 
+@pytest.mark.parametrize("sampler", [0, 1])
+def test_refinement_matches_oracle(small_scene, sampler, parity_log):
+    """pm_refine from the same depth map and view selection as the oracle's restatement: the
+    hypotheses are the same FP32 numbers, so only near-ties between FP32 and FP64 mean costs
+    may pick differently; at least 99.5% of depths within 0.1% (most bit-identical)."""
+    eng = make_engine(small_scene, sampler=sampler)
+    orc = oracle_for(eng, small_scene)
+    eng.run()
+    d0 = eng.depth().astype(np.float64)
+    vs = eng.view_selection()
+    S = small_scene.workload.num_samples
+    eng.refine(10, 0.05, 77, S, 0)
+    gd = eng.depth()
+    od = d0.copy()
+    orc.refine(od, vs, S, 10, 0.05, 77, 0)
+    rel = np.abs(gd - od) / od
+    within = float(np.mean(rel <= 1e-3))
+    identical = float(np.mean(gd == od.astype(np.float32)))
+    changed = float(np.mean(gd != d0.astype(np.float32)))
+    parity_log(f"refine_plane3_320x240_sampler{sampler}", within_0p1pct=within, bit_identical=identical,
+               changed=changed)
+    assert within >= 0.995 and identical >= 0.99
+    assert changed > 0.02
+    eng.close()
+
+
 def test_texture_peak_is_plausible(engine_lib):
     """The measured texture-filtering rate the bench reports the sweep kernel against: between
     1 and 5 bilinear samples per clock per SM."""

@@ -186,3 +186,31 @@ def _params(w):
     p.prefilter, p.num_iterations, p.orientation_x, p.orientation_z = w.prefilter, w.iterations, 0.0, 1.0
     p.seed, p.quirks = w.seed, 1
     return p
+
+
+def test_refinement_never_raises_the_sampled_views_mean_cost(oracle_lib):
+    """The refinement restatement: with no trials or no sampled views a depth stays; otherwise
+    the mean cost over the pixel's sampled views never rises, and depths stay in range."""
+    from patchmatch_cuda_gb300 import scene
+    w = scene.Workload("cpu_small", 96, 72, 3, 3, 2, 2.0, 8.0, 3, 0, seed=9)
+    sv = scene.make_views(w)
+    o = O.from_images(sv.images, sv.ref_id, _params(w))
+    d, c, vs, _ = o.run(w.iterations, w.num_samples)
+    d = d.astype(np.float32).astype(np.float64)
+    S = w.num_samples
+    same = d.copy()
+    assert o.refine(same, vs, S, 0, 0.05, 99, 0) > 0 and np.array_equal(same, d)
+    none = np.full_like(vs, 255)
+    same = d.copy()
+    assert o.refine(same, none, S, 10, 0.05, 99, 0) == 0 and np.array_equal(same, d)
+    r = d.copy()
+    o.refine(r, vs, S, 10, 0.2, 99, 0)
+    assert r.min() >= w.depth_near and r.max() <= w.depth_far
+    changed = np.argwhere(r != d)
+    assert len(changed) > 0.02 * d.size
+    rng = np.random.default_rng(0)
+    for y, x in changed[rng.choice(len(changed), 40, replace=False)]:
+        views = [int(v) for v in vs[:S, y, x] if v < w.n_src]
+        before = np.mean([o.ncc(int(x), int(y), v, float(d[y, x]), 0) for v in views])
+        after = np.mean([o.ncc(int(x), int(y), v, float(r[y, x]), 0) for v in views])
+        assert after < before
