@@ -332,6 +332,8 @@ def run_ours(args):
     total_ms, total_evals = allreduce_max_sum(world, sum(step_ms), float(evals_per_map * args.steps))
     depth = eng.depth()
     bad = scene.bad_pixel_rate(depth, sv.gt_depth)
+    rel_err = np.abs(depth - sv.gt_depth) / sv.gt_depth
+    rel_err = rel_err[np.isfinite(rel_err)]
 
     # dominant kernel: every sweep of one schedule timed on the engine's stream
     eng.init_depth()
@@ -383,13 +385,19 @@ def run_ours(args):
     variants = {}
     for name, over in [("f32_texels_box_prefilter", dict(prefilter=1)),
                        ("f16_texels_box_prefilter", dict(prefilter=1, precision=1)),
-                       ("exact_sampler", dict(sampler=0))]:
+                       ("exact_sampler", dict(sampler=0)),
+                       # slanted planes per pixel (no counterpart in the reference)
+                       ("slanted_planes", dict(planes=1))]:
         ev = Engine(sv.images, sv.ref_id, wl.params(gpu_id=local, **over))
         ev.run()
         ev.run()
         st = ev.stats()
+        dv = ev.depth()
+        rel = np.abs(dv - sv.gt_depth) / sv.gt_depth
         variants[name] = {"ms_per_depth_map": st.ms_total, "g_cost_evals_per_s": st.cost_evals / st.ms_total / 1e6,
-                          "bad_pixel_pct_1pct": round(100 * scene.bad_pixel_rate(ev.depth(), sv.gt_depth), 3)}
+                          "bad_pixel_pct_1pct": round(100 * scene.bad_pixel_rate(dv, sv.gt_depth), 3),
+                          "bad_pixel_pct_0p2pct": round(100 * float(np.mean(rel[np.isfinite(rel)] > 0.002)), 3),
+                          "median_rel_err_pct": round(100 * float(np.median(rel[np.isfinite(rel)])), 4)}
         ev.close()
     learned = learned_vs_plain(sv, wl, local, flush, max(args.steps, 3))
     cpu = None
@@ -415,6 +423,8 @@ def run_ours(args):
                 "sampler": "texture-unit bilinear (the reference's fetch)" if params.sampler == 1 else "exact gather",
                 "ms_per_depth_map": total_ms / args.steps, "cost_evals_per_depth_map": evals_per_map,
                 "bad_pixel_pct_1pct": round(100 * bad, 3),
+                "bad_pixel_pct_0p2pct": round(100 * float(np.mean(rel_err > 0.002)), 3),
+                "median_rel_err_pct": round(100 * float(np.median(rel_err)), 4),
                 "l2": "flushed before each depth map (256 MiB write, outside the timed events)",
                 "threads_per_line": tpl,
             },

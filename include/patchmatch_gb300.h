@@ -138,6 +138,19 @@ typedef struct pm_params {
                                       the reference's never-launched depthRefinement
                                       (patchMatch.cu:717-773) with 10 trials, sigma 0.05      */
     float refine_sigma;            /* depth units (default 0.05)                              */
+    int planes;                    /* 0 (default): one plane normal for every pixel, the
+                                      reference's orientationX/Z (patchMatch.cu:32,
+                                      main.cpp:65-76). 1: no counterpart in the reference; a
+                                      slanted plane per pixel, depth plus slopes (a, b) with
+                                      normal ~ (a, b, 1) in the reference camera: random
+                                      initial slopes, the previous step's plane carried to
+                                      each pixel, and a random hypothesis that is a uniform
+                                      depth, uniform slopes or a local perturbation of both.
+                                      orientation_x/z are then unused                        */
+    float plane_depth_step;        /* planes: relative half-width of the depth perturbation
+                                      in sweep k, x 2^(-k/4) (default 0.02)                  */
+    float plane_slope_step;        /* planes: half-width of the slope perturbation, x 2^(-k/4)
+                                      (default 0.25)                                         */
 } pm_params;
 
 #define PM_MAX_REFINE_TRIALS 256
@@ -228,6 +241,17 @@ pm_status pm_get_source_texels(pm_handle *h, int view, float *dst);
 /* computeNCC (patchMatch.cu:433-611) for n (x, y, view, depth, axis) tuples. */
 pm_status pm_eval_costs(pm_handle *h, int n, const int *xs, const int *ys, const int *views,
                         const float *depths, const int *axes, float *out);
+/* Slanted-plane mode (pm_params.planes = 1; no counterpart in the reference, whose one plane
+ * normal is a constant, patchMatch.cu:32): the per-pixel plane slopes (a, b) as height*width*2
+ * floats, row-major, and the unit normals (a, b, 1)/|(a, b, 1)| in the reference camera as
+ * height*width*3 floats. PM_ERR_STATE when the handle was created without planes. */
+pm_status pm_get_slopes(pm_handle *h, float *dst);
+pm_status pm_set_slopes(pm_handle *h, const float *src);
+pm_status pm_get_normals(pm_handle *h, float *dst);
+/* computeNCC for n (x, y, view, depth, slopes, axis) tuples of a slanted-plane handle:
+ * slopes holds (a, b) per query. */
+pm_status pm_eval_costs_planes(pm_handle *h, int n, const int *xs, const int *ys, const int *views,
+                               const float *depths, const float *slopes, const int *axes, float *out);
 /* Bilinear source fetch of patchMatch.cu:543 at source coordinates (xs, ys). */
 pm_status pm_sample_source(pm_handle *h, int view, int n, const float *xs, const float *ys,
                            float *out);

@@ -169,6 +169,21 @@ void pmo_init_relative(const double k_ref[9], const double r_ref[9], const doubl
     out_inv_k[3] = k_ref_inv[5];
 }
 
+void pmo_translation_term(const double r_ref[9], const double t_ref[3], const double k_src[9],
+                          const double r_src[9], const double t_src[3], double out_e[3])
+{
+    double c_ref[3], c_src[3], t_rel[3];
+    for (int i = 0; i < 3; ++i) {
+        c_ref[i] = -(r_ref[i] * t_ref[0] + r_ref[3 + i] * t_ref[1] + r_ref[6 + i] * t_ref[2]);
+        c_src[i] = -(r_src[i] * t_src[0] + r_src[3 + i] * t_src[1] + r_src[6 + i] * t_src[2]);
+    }
+    const double dc[3] = {c_src[0] - c_ref[0], c_src[1] - c_ref[1], c_src[2] - c_ref[2]};
+    for (int i = 0; i < 3; ++i)
+        t_rel[i] = r_src[3 * i] * dc[0] + r_src[3 * i + 1] * dc[1] + r_src[3 * i + 2] * dc[2];
+    for (int i = 0; i < 3; ++i)
+        out_e[i] = k_src[3 * i] * t_rel[0] + k_src[3 * i + 1] * t_rel[1] + k_src[3 * i + 2] * t_rel[2];
+}
+
 /* ------------------------------------------------------------------------------------
  * GaussianBlurCUDA (GaussianBlurCUDA.cu:73-199): separable row then column filter of a
  * float image with zero border. Width = (int)(5*sigma), made odd, clamped to [5, 45]
@@ -325,15 +340,10 @@ static float device_scale(const pmo_problem *p, int x)
                  (float)p->orientation[2]);
 }
 
-/* T = H1 - s H2 with s = 1/(depth scale), the texture's half-texel offset folded into the
- * first two rows, evaluated at the window origin (ox, oy): out[0..8] = c0 (3), c1 (3), base (3). */
-static void device_warp(const pmo_problem *p, int view, float depth, float scale, float ox,
-                        float oy, float out[9])
+/* The texture's half-texel offset folded into the first two rows of T, evaluated at the
+ * window origin (ox, oy): out[0..8] = c0 (3), c1 (3), base (3). */
+static void warp_tail(float t[9], float ox, float oy, float out[9])
 {
-    const double *hh = p->hh + 18 * (size_t)view;
-    const float s = f_rcp(f_mul(depth, scale));
-    float t[9];
-    for (int i = 0; i < 9; ++i) t[i] = f_fma(-s, (float)hh[9 + i], (float)hh[i]);
     for (int i = 0; i < 3; ++i) {
         t[i] = f_fma(0.5f, t[6 + i], t[i]);
         t[3 + i] = f_fma(0.5f, t[6 + i], t[3 + i]);
@@ -343,6 +353,48 @@ static void device_warp(const pmo_problem *p, int view, float depth, float scale
     out[6] = f_fma(t[0], ox, f_fma(t[1], oy, t[2]));
     out[7] = f_fma(t[3], ox, f_fma(t[4], oy, t[5]));
     out[8] = f_fma(t[6], ox, f_fma(t[7], oy, t[8]));
+}
+
+/* T = H1 - s H2 with s = 1/(depth scale). */
+static void device_warp(const pmo_problem *p, int view, float depth, float scale, float ox,
+                        float oy, float out[9])
+{
+    const double *hh = p->hh + 18 * (size_t)view;
+    const float s = f_rcp(f_mul(depth, scale));
+    float t[9];
+    for (int i = 0; i < 9; ++i) t[i] = f_fma(-s, (float)hh[9 + i], (float)hh[i]);
+    warp_tail(t, ox, oy, out);
+}
+
+/* Slanted-plane mode: g = (a ik00, b ik11, a ik02 + b ik12 + 1) = K_r^-T n for n = (a, b, 1),
+ * and the plane scale s = g . (x + 1/2, y + 1/2, 1) floored at PMO_SCALE_MIN, in the engine's
+ * single-precision steps. */
+typedef struct { float g0, g1, g2, s; } plane_terms_t;
+
+static inline plane_terms_t plane_terms(const pmo_problem *p, float a, float b, int x, int y)
+{
+    plane_terms_t r;
+    r.g0 = f_mul(a, (float)p->inv_k[0]);
+    r.g1 = f_mul(b, (float)p->inv_k[2]);
+    r.g2 = f_fma(a, (float)p->inv_k[1], f_fma(b, (float)p->inv_k[3], 1.0f));
+    const float s = f_fma(r.g0, f_add((float)x, 0.5f), f_fma(r.g1, f_add((float)y, 0.5f), r.g2));
+    r.s = s < PMO_SCALE_MIN ? PMO_SCALE_MIN : s;
+    return r;
+}
+
+/* T = H1 - e g^T / (depth s), each product e_r g_c rounded to float. */
+static void device_warp_plane(const pmo_problem *p, int view, float depth, plane_terms_t G,
+                              float ox, float oy, float out[9])
+{
+    const double *hh = p->hh + 18 * (size_t)view;
+    const double *e = p->ee + 3 * (size_t)view;
+    const float inv = f_rcp(f_mul(depth, G.s));
+    const float g[3] = {G.g0, G.g1, G.g2};
+    float t[9];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c)
+            t[3 * r + c] = f_fma(-inv, f_mul((float)e[r], g[c]), (float)hh[3 * r + c]);
+    warp_tail(t, ox, oy, out);
 }
 
 /* Plane scale s = n^T K^-1 (x + 1/2, y + 1/2, 1): patchMatch.cu:798-800, :876-883 with
@@ -366,18 +418,33 @@ static inline real plane_scale(const pmo_problem *p, int x)
  * product is 0; else 1 - (sum(I I') - sum(I) sum(I')/n) / sqrt(c1 c2).
  * ---------------------------------------------------------------------------------- */
 static real ncc_eval(const pmo_problem *p, const double *sum_i, const double *sum_ii,
-                     int x, int y, int view, real depth, int axis, real scale)
+                     int x, int y, int view, real depth, int axis, real scale, const float *plane)
 {
     const int hw = p->half_window, w = 2 * hw + 1, W = p->width, H = p->height;
     const double *hh = p->hh + 18 * (size_t)view;
     real t[9];
-    for (int i = 0; i < 9; ++i) t[i] = (real)hh[i] - (real)hh[9 + i] / depth / scale;
+    plane_terms_t G = {0, 0, 0, 0};
+    if (plane) {
+        /* slanted plane (a, b) = plane[0..1]: T = H1 - e g^T / (depth s) */
+        G = plane_terms(p, plane[0], plane[1], x, y);
+        const double *e = p->ee + 3 * (size_t)view;
+        const real g[3] = {(real)G.g0, (real)G.g1, (real)G.g2};
+        const real rho = depth * (real)G.s;
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) t[3 * r + c] = (real)hh[3 * r + c] - (real)e[r] * g[c] / rho;
+    } else {
+        for (int i = 0; i < 9; ++i) t[i] = (real)hh[i] - (real)hh[9 + i] / depth / scale;
+    }
     const float *src = p->src[view];
     const int sw = p->src_width[view], sh = p->src_height[view];
     float dw[9];
-    if (p->sampler == 1)
-        device_warp(p, view, (float)depth, device_scale(p, x), (float)(x - hw) + 0.5f,
-                    (float)(y - hw) + 0.5f, dw);
+    if (p->sampler == 1) {
+        if (plane)
+            device_warp_plane(p, view, (float)depth, G, (float)(x - hw) + 0.5f, (float)(y - hw) + 0.5f, dw);
+        else
+            device_warp(p, view, (float)depth, device_scale(p, x), (float)(x - hw) + 0.5f,
+                        (float)(y - hw) + 0.5f, dw);
+    }
     int lead = 0;
     if (p->quirks) lead = axis == 0 ? (hw - x > 0 ? hw - x : 0) : (hw - y > 0 ? hw - y : 0);
 
@@ -436,7 +503,24 @@ static real ncc_eval(const pmo_problem *p, const double *sum_i, const double *su
 double pmo_ncc(const pmo_problem *p, const double *sum_i, const double *sum_ii,
                int x, int y, int view, double depth, int axis)
 {
-    return (double)ncc_eval(p, sum_i, sum_ii, x, y, view, (real)depth, axis, plane_scale(p, x));
+    return (double)ncc_eval(p, sum_i, sum_ii, x, y, view, (real)depth, axis, plane_scale(p, x), NULL);
+}
+
+double pmo_ncc_plane(const pmo_problem *p, const double *sum_i, const double *sum_ii,
+                     int x, int y, int view, double depth, float a, float b, int axis)
+{
+    const float ab[2] = {a, b};
+    return (double)ncc_eval(p, sum_i, sum_ii, x, y, view, (real)depth, axis, 0, ab);
+}
+
+void pmo_ncc_plane_batch(const pmo_problem *p, const double *sum_i, const double *sum_ii, int n,
+                         const int *xs, const int *ys, const int *views, const double *depths,
+                         const float *slopes, const int *axes, double *out)
+{
+    #pragma omp parallel for schedule(dynamic, 64)
+    for (int i = 0; i < n; ++i)
+        out[i] = (double)ncc_eval(p, sum_i, sum_ii, xs[i], ys[i], views[i], (real)depths[i], axes[i], 0,
+                                  slopes + 2 * (size_t)i);
 }
 
 void pmo_ncc_batch(const pmo_problem *p, const double *sum_i, const double *sum_ii, int n,
@@ -448,9 +532,9 @@ void pmo_ncc_batch(const pmo_problem *p, const double *sum_i, const double *sum_
         out[i] = pmo_ncc(p, sum_i, sum_ii, xs[i], ys[i], views[i], depths[i], axes[i]);
 }
 
-long long pmo_refine(const pmo_problem *p, const double *sum_i, const double *sum_ii, double *depth,
-                     const unsigned char *view_sel, int num_samples, int trials, float sigma,
-                     uint32_t sweep_id, int axis)
+static long long refine_impl(const pmo_problem *p, const double *sum_i, const double *sum_ii, double *depth,
+                             const float *slopes, const unsigned char *view_sel, int num_samples, int trials,
+                             float sigma, uint32_t sweep_id, int axis)
 {
     const int W = p->width, H = p->height, V = p->n_src;
     const int npix = W * H;
@@ -468,9 +552,10 @@ long long pmo_refine(const pmo_problem *p, const double *sum_i, const double *su
         }
         if (nv == 0) continue;
         const real scale = plane_scale(p, x);
+        const float *pl = slopes ? slopes + 2 * (size_t)pix : NULL;
         const float d0 = (float)depth[pix];
         real best_cost = 0;
-        for (int k = 0; k < nv; ++k) best_cost += ncc_eval(p, sum_i, sum_ii, x, y, views[k], (real)d0, axis, scale);
+        for (int k = 0; k < nv; ++k) best_cost += ncc_eval(p, sum_i, sum_ii, x, y, views[k], (real)d0, axis, scale, pl);
         best_cost /= (real)nv;
         evals += nv;
         float best = d0;
@@ -486,7 +571,7 @@ long long pmo_refine(const pmo_problem *p, const double *sum_i, const double *su
             const float dn = f_add(d0, f_mul(f_mul(z, sqrt3), sigma));
             if (!(dn >= d_lo && dn <= d_hi)) continue;
             real c = 0;
-            for (int k = 0; k < nv; ++k) c += ncc_eval(p, sum_i, sum_ii, x, y, views[k], (real)dn, axis, scale);
+            for (int k = 0; k < nv; ++k) c += ncc_eval(p, sum_i, sum_ii, x, y, views[k], (real)dn, axis, scale, pl);
             c /= (real)nv;
             evals += nv;
             if (c < best_cost) {
@@ -497,6 +582,20 @@ long long pmo_refine(const pmo_problem *p, const double *sum_i, const double *su
         depth[pix] = (double)best;
     }
     return evals;
+}
+
+long long pmo_refine(const pmo_problem *p, const double *sum_i, const double *sum_ii, double *depth,
+                     const unsigned char *view_sel, int num_samples, int trials, float sigma,
+                     uint32_t sweep_id, int axis)
+{
+    return refine_impl(p, sum_i, sum_ii, depth, NULL, view_sel, num_samples, trials, sigma, sweep_id, axis);
+}
+
+long long pmo_refine_planes(const pmo_problem *p, const double *sum_i, const double *sum_ii,
+                            double *depth, const float *slopes, const unsigned char *view_sel,
+                            int num_samples, int trials, float sigma, uint32_t sweep_id, int axis)
+{
+    return refine_impl(p, sum_i, sum_ii, depth, slopes, view_sel, num_samples, trials, sigma, sweep_id, axis);
 }
 
 /* ------------------------------------------------------------------------------------
@@ -579,10 +678,26 @@ void pmo_init_depth(const pmo_problem *p, double *depth)
     }
 }
 
-/* computeAllCostGivenDepth<W> (patchMatch.cu:775-816): every view's cost at the current
- * depth. The reference runs it on the transposed maps (isRotated = true, :338-343). */
-long long pmo_initial_costs(const pmo_problem *p, const double *sum_i, const double *sum_ii,
-                            const double *depth, double *cost)
+/* Slanted-plane mode: initial slopes uniform in [-PMO_SLOPE_DRAW, PMO_SLOPE_DRAW]^2 from words
+ * 1 and 2 of the initial-depth counter (word 0 is the depth). */
+void pmo_init_planes(const pmo_problem *p, float *slopes)
+{
+    const int n = p->width * p->height;
+    const uint32_t key[2] = {(uint32_t)p->seed, (uint32_t)(p->seed >> 32)};
+    #pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; ++i) {
+        const uint32_t ctr[4] = {(uint32_t)i, 0xFFFFFFFFu, (uint32_t)PMO_RNG_INIT << 16, p->batch_id};
+        uint32_t o[4];
+        pmo_philox4x32_10(ctr, key, o);
+        for (int k = 0; k < 2; ++k) {
+            const float u = (float)((o[1 + k] >> 8) + 1u) * (1.0f / 16777216.0f);
+            slopes[2 * (size_t)i + k] = f_mul(PMO_SLOPE_DRAW, f_fma(2.0f, u, -1.0f));
+        }
+    }
+}
+
+static long long initial_costs_impl(const pmo_problem *p, const double *sum_i, const double *sum_ii,
+                                    const double *depth, const float *slopes, double *cost)
 {
     const int W = p->width, H = p->height, V = p->n_src;
     #pragma omp parallel for schedule(dynamic, 4)
@@ -590,11 +705,26 @@ long long pmo_initial_costs(const pmo_problem *p, const double *sum_i, const dou
         for (int x = 0; x < W; ++x) {
             real scale = plane_scale(p, x);
             size_t pix = (size_t)y * W + x;
+            const float *pl = slopes ? slopes + 2 * pix : NULL;
             for (int v = 0; v < V; ++v)
                 cost[pix * V + v] = (double)ncc_eval(p, sum_i, sum_ii, x, y, v,
-                                                     (real)depth[pix], 1, scale);
+                                                     (real)depth[pix], 1, scale, pl);
         }
     return (long long)W * H * V;
+}
+
+long long pmo_initial_costs_planes(const pmo_problem *p, const double *sum_i, const double *sum_ii,
+                                   const double *depth, const float *slopes, double *cost)
+{
+    return initial_costs_impl(p, sum_i, sum_ii, depth, slopes, cost);
+}
+
+/* computeAllCostGivenDepth<W> (patchMatch.cu:775-816): every view's cost at the current
+ * depth. The reference runs it on the transposed maps (isRotated = true, :338-343). */
+long long pmo_initial_costs(const pmo_problem *p, const double *sum_i, const double *sum_ii,
+                            const double *depth, double *cost)
+{
+    return initial_costs_impl(p, sum_i, sum_ii, depth, NULL, cost);
 }
 
 /* ------------------------------------------------------------------------------------
@@ -615,9 +745,9 @@ long long pmo_initial_costs(const pmo_problem *p, const double *sum_i, const dou
  *     views (:1159-1163).
  * Returns the number of NCC evaluations the algorithm performed.
  * ---------------------------------------------------------------------------------- */
-long long pmo_sweep(const pmo_problem *p, const double *sum_i, const double *sum_ii,
-                    double *depth, double *cost, int dir, uint32_t sweep_id, int num_samples,
-                    unsigned char *view_sel, int line_begin, int line_end)
+static long long sweep_impl(const pmo_problem *p, const double *sum_i, const double *sum_ii,
+                            double *depth, float *slopes, double *cost, int dir, uint32_t sweep_id,
+                            int num_samples, unsigned char *view_sel, int line_begin, int line_end)
 {
     const int W = p->width, H = p->height, V = p->n_src, S = num_samples;
     const int rotated = (dir == PMO_DIR_LR || dir == PMO_DIR_RL);
@@ -628,6 +758,12 @@ long long pmo_sweep(const pmo_problem *p, const double *sum_i, const double *sum
     const real a2 = alpha_sq(p->sp_alpha);
     const real u_emit = uniform_emission(a2);
     const float perturb = p->perturbation > 0.0f ? p->perturbation * exp2f(-0.25f * (float)sweep_id) : 0.0f;
+    /* slanted-plane mode: the local search's widths in this sweep, the depth range in float */
+    const int planar = slopes != NULL;
+    const float dstep = p->plane_depth_step * exp2f(-0.25f * (float)sweep_id);
+    const float sstep = p->plane_slope_step * exp2f(-0.25f * (float)sweep_id);
+    const float d_lo = (float)p->depth_near;
+    const float d_hi = f_add(d_lo, (float)((double)(float)p->depth_far - (double)d_lo));
     if (line_begin < 0) line_begin = 0;
     if (line_end < 0 || line_end > nlines) line_end = nlines;
     long long evals = 0;
@@ -667,6 +803,13 @@ long long pmo_sweep(const pmo_problem *p, const double *sum_i, const double *sum
                 }
             }
             real d_former = (real)depth[PY(0) * W + PX(0)];
+            /* slanted-plane mode: the previous step's plane and pixel */
+            float a_former = 0, b_former = 0;
+            int x_former = PX(0), y_former = PY(0);
+            if (planar) {
+                a_former = slopes[2 * ((size_t)PY(0) * W + PX(0))];
+                b_former = slopes[2 * ((size_t)PY(0) * W + PX(0)) + 1];
+            }
             /* 3. propagation */
             for (int k = 1; k < nsteps; ++k) {
                 const int x = PX(k), y = PY(k);
@@ -688,15 +831,48 @@ long long pmo_sweep(const pmo_problem *p, const double *sum_i, const double *sum
 
                 const real d_cur = (real)depth[pix];
                 real d_rand;
+                /* plane hypotheses (slanted-plane mode): former, current, random */
+                float pl_f[2] = {0, 0}, pl_c[2] = {0, 0}, pl_r[2] = {0, 0};
+                real d_prop = d_former;
                 {
                     const uint32_t ctr[4] = {(uint32_t)pix, sweep_id, ((uint32_t)PMO_RNG_RAND_DEPTH << 16), p->batch_id};
                     const uint32_t key[2] = {(uint32_t)p->seed, (uint32_t)(p->seed >> 32)};
                     uint32_t o[4];
                     pmo_philox4x32_10(ctr, key, o);
-                    const float u = (float)((o[0] >> 8) + 1u) * (1.0f / 16777216.0f);
-                    const float u2 = (float)((o[1] >> 8) + 1u) * (1.0f / 16777216.0f);
+                    float uw[4];
+                    for (int k = 0; k < 4; ++k) uw[k] = (float)((o[k] >> 8) + 1u) * (1.0f / 16777216.0f);
+                    const float u = uw[0], u2 = uw[1];
                     d_rand = (real)float_depth((double)u, p->depth_near, p->depth_far);
-                    if (perturb > 0.0f && u2 >= 0.5f) {
+                    if (planar) {
+                        /* the previous step's plane carried to this pixel: d s_prev / s_here */
+                        pl_f[0] = a_former;
+                        pl_f[1] = b_former;
+                        const plane_terms_t gq = plane_terms(p, a_former, b_former, x_former, y_former);
+                        const plane_terms_t gp = plane_terms(p, a_former, b_former, x, y);
+                        float df = f_mul((float)d_former, f_mul(gq.s, f_rcp(gp.s)));
+                        df = df < d_lo ? d_lo : (df > d_hi ? d_hi : df);
+                        d_prop = (real)df;
+                        pl_c[0] = slopes[2 * (size_t)pix];
+                        pl_c[1] = slopes[2 * (size_t)pix + 1];
+                        if (u2 < 0.33333334f) {
+                            /* uniform depth, current slopes (the reference's random depth) */
+                            pl_r[0] = pl_c[0];
+                            pl_r[1] = pl_c[1];
+                        } else if (u2 < 0.6666667f) {
+                            /* current depth, uniform slopes */
+                            d_rand = d_cur;
+                            pl_r[0] = f_mul(PMO_SLOPE_DRAW, f_fma(2.0f, uw[2], -1.0f));
+                            pl_r[1] = f_mul(PMO_SLOPE_DRAW, f_fma(2.0f, uw[3], -1.0f));
+                        } else {
+                            /* local perturbation of depth and slopes */
+                            float dr = f_mul((float)d_cur, f_fma(dstep, f_fma(2.0f, u, -1.0f), 1.0f));
+                            d_rand = (real)(dr < d_lo ? d_lo : (dr > d_hi ? d_hi : dr));
+                            for (int k = 0; k < 2; ++k) {
+                                const float sl = f_fma(sstep, f_fma(2.0f, uw[2 + k], -1.0f), pl_c[k]);
+                                pl_r[k] = sl < -PMO_SLOPE_MAX ? -PMO_SLOPE_MAX : (sl > PMO_SLOPE_MAX ? PMO_SLOPE_MAX : sl);
+                            }
+                        }
+                    } else if (perturb > 0.0f && u2 >= 0.5f) {
                         /* the engine's local search, in its single-precision arithmetic */
                         const float lo = (float)p->depth_near;
                         const float hi = f_add(lo, (float)((double)(float)p->depth_far - (double)lo));
@@ -705,6 +881,7 @@ long long pmo_sweep(const pmo_problem *p, const double *sum_i, const double *sum
                         d_rand = (real)dr;
                     }
                 }
+                const float *plf = planar ? pl_f : NULL, *plr = planar ? pl_r : NULL;
                 real c3[3] = {0, 0, 0};
                 int tested = 0;
                 for (int j = 0; j < S; ++j) {
@@ -715,9 +892,9 @@ long long pmo_sweep(const pmo_problem *p, const double *sum_i, const double *sum
                     vsel[j] = view;
                     if (view < 0) continue;
                     ++tested;
-                    c3[0] += ncc_eval(p, sum_i, sum_ii, x, y, view, d_former, axis, scale);
+                    c3[0] += ncc_eval(p, sum_i, sum_ii, x, y, view, d_prop, axis, scale, plf);
                     c3[1] += c_old[view];
-                    c3[2] += ncc_eval(p, sum_i, sum_ii, x, y, view, d_rand, axis, scale);
+                    c3[2] += ncc_eval(p, sum_i, sum_ii, x, y, view, d_rand, axis, scale, plr);
                 }
                 evals += 2 * tested;
                 int idx = 1;
@@ -726,12 +903,20 @@ long long pmo_sweep(const pmo_problem *p, const double *sum_i, const double *sum
                     c3[0] *= inv; c3[1] *= inv; c3[2] *= inv;
                     idx = find_min_cost(c3);
                 }
-                const real best = idx == 0 ? d_former : (idx == 1 ? d_cur : d_rand);
+                const real best = idx == 0 ? d_prop : (idx == 1 ? d_cur : d_rand);
+                const float *pl_best = idx == 0 ? pl_f : (idx == 1 ? pl_c : pl_r);
                 depth[pix] = (double)best;
                 d_former = best;
+                if (planar) {
+                    a_former = slopes[2 * (size_t)pix] = pl_best[0];
+                    b_former = slopes[2 * (size_t)pix + 1] = pl_best[1];
+                    x_former = x;
+                    y_former = y;
+                }
                 if (idx != 1) {
                     for (int v = 0; v < V; ++v)
-                        cpix[v] = (double)ncc_eval(p, sum_i, sum_ii, x, y, v, best, axis, scale);
+                        cpix[v] = (double)ncc_eval(p, sum_i, sum_ii, x, y, v, best, axis, scale,
+                                                   planar ? pl_best : NULL);
                     evals += V;
                 }
                 for (int v = 0; v < V; ++v) {
@@ -753,6 +938,22 @@ long long pmo_sweep(const pmo_problem *p, const double *sum_i, const double *sum
     return evals;
 }
 
+long long pmo_sweep(const pmo_problem *p, const double *sum_i, const double *sum_ii,
+                    double *depth, double *cost, int dir, uint32_t sweep_id, int num_samples,
+                    unsigned char *view_sel, int line_begin, int line_end)
+{
+    return sweep_impl(p, sum_i, sum_ii, depth, NULL, cost, dir, sweep_id, num_samples, view_sel, line_begin,
+                      line_end);
+}
+
+long long pmo_sweep_planes(const pmo_problem *p, const double *sum_i, const double *sum_ii,
+                           double *depth, float *slopes, double *cost, int dir, uint32_t sweep_id,
+                           int num_samples, unsigned char *view_sel, int line_begin, int line_end)
+{
+    return sweep_impl(p, sum_i, sum_ii, depth, slopes, cost, dir, sweep_id, num_samples, view_sel, line_begin,
+                      line_end);
+}
+
 /* PatchMatch::run<W> (patchMatch.cu:307-394): iteration 0 samples one view and first
  * computes every cost at the initial depth; each iteration sweeps left-to-right,
  * top-to-bottom, right-to-left, bottom-to-top; the last sweep of the last iteration
@@ -770,6 +971,24 @@ long long pmo_run(const pmo_problem *p, int iterations, int num_samples,
             unsigned char *vs = (it == iterations - 1 && d == PMO_DIR_BT) ? view_sel : NULL;
             evals += pmo_sweep(p, sum_i, sum_ii, depth, cost, d, (uint32_t)(4 * it + d), s, vs,
                                0, -1);
+        }
+    }
+    return evals;
+}
+
+long long pmo_run_planes(const pmo_problem *p, int iterations, int num_samples,
+                         const double *sum_i, const double *sum_ii, double *depth, float *slopes,
+                         double *cost, unsigned char *view_sel)
+{
+    long long evals = 0;
+    pmo_init_depth(p, depth);
+    pmo_init_planes(p, slopes);
+    for (int it = 0; it < iterations; ++it) {
+        int s = it == 0 ? 1 : num_samples;
+        if (it == 0) evals += initial_costs_impl(p, sum_i, sum_ii, depth, slopes, cost);
+        for (int d = 0; d < 4; ++d) {
+            unsigned char *vs = (it == iterations - 1 && d == PMO_DIR_BT) ? view_sel : NULL;
+            evals += sweep_impl(p, sum_i, sum_ii, depth, slopes, cost, d, (uint32_t)(4 * it + d), s, vs, 0, -1);
         }
     }
     return evals;

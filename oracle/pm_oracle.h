@@ -69,7 +69,24 @@ typedef struct pmo_problem {
                                        engine's local search: half of the pixels (second
                                        Philox word >= 1/2) draw within +-perturbation x
                                        2^(-sweep/4) of their current depth                */
+    int planes;                     /* 0: one plane normal for every pixel, the reference's
+                                       orientation (patchMatch.cu:32, main.cpp:65-76).
+                                       1: a slanted plane per pixel, n ~ (a, b, 1) in the
+                                       reference camera (no counterpart in the reference) */
+    const double *ee;               /* planes: n_src*3, e = K_s T_rel, the column vector of
+                                       H2 = K_s T_rel n^T K_r^-1 (image.cpp:4-13)           */
+    float plane_depth_step;         /* planes: relative half-width of the local search's depth
+                                       perturbation at sweep 0 (scaled by 2^(-sweep/4))      */
+    float plane_slope_step;         /* planes: half-width of its slope perturbation at sweep 0 */
 } pmo_problem;
+
+/* Slanted-plane mode. A pixel's plane is its depth d (reference-camera z) and slopes (a, b):
+ * normal n ~ (a, b, 1), so n . X = d s with the plane scale
+ * s = a (ik00 (x + 1/2) + ik02) + b (ik11 (y + 1/2) + ik12) + 1 (floored at PMO_SCALE_MIN), and
+ * the homography is H1 - e g^T / (d s) with g = (a ik00, b ik11, a ik02 + b ik12 + 1). */
+#define PMO_SLOPE_DRAW 1.0f     /* random slopes are uniform in [-1, 1]^2                  */
+#define PMO_SLOPE_MAX 2.0f      /* perturbed slopes clamp to [-2, 2]                       */
+#define PMO_SCALE_MIN 0.0625f
 
 void pmo_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 double pmo_uniform(uint64_t seed, uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3);
@@ -78,6 +95,9 @@ void pmo_init_relative(const double k_ref[9], const double r_ref[9], const doubl
                        const double k_src[9], const double r_src[9], const double t_src[3],
                        double orientation_x, double orientation_z,
                        double out_hh[18], double out_inv_k[4]);
+/* e = K_s T_rel = K_s R_s (C_s - C_r) (image.cpp:4-13), the plane-mode translation term. */
+void pmo_translation_term(const double r_ref[9], const double t_ref[3], const double k_src[9],
+                          const double r_src[9], const double t_src[3], double out_e[3]);
 
 int pmo_prefilter(const float *in, int width, int height, int mode, float sigma, float *out);
 void pmo_box_moments(const float *img, int width, int height, int half_window,
@@ -110,6 +130,31 @@ long long pmo_refine(const pmo_problem *p, const double *sum_i, const double *su
 long long pmo_run(const pmo_problem *p, int iterations, int num_samples,
                   const double *sum_i, const double *sum_ii,
                   double *depth, double *cost, unsigned char *view_sel);
+
+/* Slanted-plane mode (p->planes = 1): slopes hold (a, b) per pixel, height*width*2 floats.
+ * Initial slopes are uniform in [-PMO_SLOPE_DRAW, PMO_SLOPE_DRAW]^2 from words 1 and 2 of the
+ * initial-depth counter. In a sweep the three hypotheses are: the previous step's plane carried
+ * to this pixel (d' = d s_prev / s_here under its slopes), the current plane, and a random one
+ * from the four words of the random-depth counter: word 1 < 1/3 a uniform depth with the
+ * current slopes (the reference's random depth); < 2/3 the current depth with uniform slopes;
+ * else a local perturbation of both (plane_depth_step, plane_slope_step, each x 2^(-sweep/4)). */
+void pmo_init_planes(const pmo_problem *p, float *slopes);
+double pmo_ncc_plane(const pmo_problem *p, const double *sum_i, const double *sum_ii,
+                     int x, int y, int view, double depth, float a, float b, int axis);
+void pmo_ncc_plane_batch(const pmo_problem *p, const double *sum_i, const double *sum_ii, int n,
+                         const int *xs, const int *ys, const int *views, const double *depths,
+                         const float *slopes, const int *axes, double *out);
+long long pmo_initial_costs_planes(const pmo_problem *p, const double *sum_i, const double *sum_ii,
+                                   const double *depth, const float *slopes, double *cost);
+long long pmo_sweep_planes(const pmo_problem *p, const double *sum_i, const double *sum_ii,
+                           double *depth, float *slopes, double *cost, int dir, uint32_t sweep_id,
+                           int num_samples, unsigned char *view_sel, int line_begin, int line_end);
+long long pmo_refine_planes(const pmo_problem *p, const double *sum_i, const double *sum_ii,
+                            double *depth, const float *slopes, const unsigned char *view_sel,
+                            int num_samples, int trials, float sigma, uint32_t sweep_id, int axis);
+long long pmo_run_planes(const pmo_problem *p, int iterations, int num_samples,
+                         const double *sum_i, const double *sum_ii, double *depth, float *slopes,
+                         double *cost, unsigned char *view_sel);
 
 /* Message updates and the tie rule, exposed for known-answer tests. */
 double pmo_msg_forward(double msg, double cost, double u_if_two, float sp_alpha);

@@ -34,7 +34,12 @@ class _Problem(C.Structure):
         ("depth_near", C.c_double), ("depth_far", C.c_double), ("sp_alpha", C.c_float),
         ("seed", C.c_uint64), ("batch_id", C.c_uint32), ("quirks", C.c_int),
         ("sampler", C.c_int), ("perturbation", C.c_float),
+        ("planes", C.c_int), ("ee", C.c_void_p), ("plane_depth_step", C.c_float),
+        ("plane_slope_step", C.c_float),
     ]
+
+# Slanted-plane mode's constants (pm_oracle.h)
+SLOPE_DRAW, SLOPE_MAX, SCALE_MIN = 1.0, 2.0, 0.0625
 
 
 _libs: dict[bool, C.CDLL] = {}
@@ -68,6 +73,19 @@ def load(fp32: bool = False) -> C.CDLL:
     lib.pmo_sweep.argtypes = [P, P, P, P, P, C.c_int, C.c_uint32, C.c_int, P, C.c_int, C.c_int]
     lib.pmo_run.restype = C.c_longlong
     lib.pmo_run.argtypes = [P, C.c_int, C.c_int, P, P, P, P, P]
+    lib.pmo_translation_term.argtypes = [P, P, P, P, P, P]
+    lib.pmo_init_planes.argtypes = [P, P]
+    lib.pmo_ncc_plane.restype = C.c_double
+    lib.pmo_ncc_plane.argtypes = [P, P, P, C.c_int, C.c_int, C.c_int, C.c_double, C.c_float, C.c_float, C.c_int]
+    lib.pmo_ncc_plane_batch.argtypes = [P, P, P, C.c_int, P, P, P, P, P, P, P]
+    lib.pmo_initial_costs_planes.restype = C.c_longlong
+    lib.pmo_initial_costs_planes.argtypes = [P, P, P, P, P, P]
+    lib.pmo_sweep_planes.restype = C.c_longlong
+    lib.pmo_sweep_planes.argtypes = [P, P, P, P, P, P, C.c_int, C.c_uint32, C.c_int, P, C.c_int, C.c_int]
+    lib.pmo_refine_planes.restype = C.c_longlong
+    lib.pmo_refine_planes.argtypes = [P, P, P, P, P, P, C.c_int, C.c_int, C.c_float, C.c_uint32, C.c_int]
+    lib.pmo_run_planes.restype = C.c_longlong
+    lib.pmo_run_planes.argtypes = [P, C.c_int, C.c_int, P, P, P, P, P, P]
     lib.pmo_msg_forward.restype = C.c_double
     lib.pmo_msg_forward.argtypes = [C.c_double, C.c_double, C.c_double, C.c_float]
     lib.pmo_msg_backward.restype = C.c_double
@@ -100,6 +118,15 @@ def init_relative(K_ref, R_ref, t_ref, K_src, R_src, t_src, nx=0.0, nz=1.0):
     ik = np.zeros(4)
     lib.pmo_init_relative(*[a.ctypes.data for a in arrs], nx, nz, hh.ctypes.data, ik.ctypes.data)
     return hh, ik
+
+
+def translation_term(R_ref, t_ref, K_src, R_src, t_src) -> np.ndarray:
+    """e = K_s R_s (C_s - C_r), the slanted-plane mode's translation term."""
+    lib = load()
+    arrs = [np.ascontiguousarray(a, np.float64).ravel() for a in (R_ref, t_ref, K_src, R_src, t_src)]
+    e = np.zeros(3)
+    lib.pmo_translation_term(*[a.ctypes.data for a in arrs], e.ctypes.data)
+    return e
 
 
 def prefilter(img: np.ndarray, mode: int, sigma: float, fp32: bool = False) -> np.ndarray:
@@ -139,7 +166,7 @@ class Oracle:
     def __init__(self, ref: np.ndarray, sources: list[np.ndarray], hh: np.ndarray, inv_k,
                  half_window: int, depth_near: float, depth_far: float, sp_alpha: float, seed: int,
                  orientation=(0.0, 0.0, 1.0), quirks: bool = True, batch_id: int = 0,
-                 fp32: bool = False, sampler: int = 0):
+                 fp32: bool = False, sampler: int = 0, ee: np.ndarray | None = None):
         self.lib = load(fp32)
         self.ref = np.ascontiguousarray(ref, np.float32)
         self.sources = [np.ascontiguousarray(s, np.float32) for s in sources]
@@ -162,6 +189,11 @@ class Oracle:
         p.seed, p.batch_id, p.quirks = seed, batch_id, int(quirks)
         p.sampler = int(sampler)
         p.perturbation = 0.0
+        # slanted-plane mode's per-view translation terms (enabled with set_planes)
+        self.ee = np.ascontiguousarray(ee if ee is not None else np.zeros((self.V, 3)), np.float64).reshape(self.V, 3)
+        p.ee = self.ee.ctypes.data
+        p.planes = 0
+        p.plane_depth_step, p.plane_slope_step = 0.0, 0.0
         self.p = p
         self.half_window = half_window
         self.sum_i, self.sum_ii = box_moments(self.ref, half_window, fp32)
@@ -224,6 +256,72 @@ class Oracle:
         return self.lib.pmo_refine(self._pp, self.sum_i.ctypes.data, self.sum_ii.ctypes.data, depth.ctypes.data,
                                    vs.ctypes.data, num_samples, trials, sigma, sweep_id, axis)
 
+    # ---- slanted-plane mode -----------------------------------------------------------
+    def set_planes(self, on: bool = True, depth_step: float = 0.0, slope_step: float = 0.0):
+        self.p.planes = int(on)
+        self.p.plane_depth_step = depth_step
+        self.p.plane_slope_step = slope_step
+
+    def init_planes(self) -> np.ndarray:
+        s = np.empty((self.H, self.W, 2), np.float32)
+        self.lib.pmo_init_planes(self._pp, s.ctypes.data)
+        return s
+
+    def ncc_plane(self, x, y, view, depth, a, b, axis) -> float:
+        return self.lib.pmo_ncc_plane(self._pp, self.sum_i.ctypes.data, self.sum_ii.ctypes.data, x, y, view, depth,
+                                      a, b, axis)
+
+    def ncc_plane_batch(self, xs, ys, views, depths, slopes, axes) -> np.ndarray:
+        xs = np.ascontiguousarray(xs, np.int32).ravel()
+        ys = np.ascontiguousarray(np.broadcast_to(ys, xs.shape), np.int32)
+        vs = np.ascontiguousarray(np.broadcast_to(views, xs.shape), np.int32)
+        ds = np.ascontiguousarray(np.broadcast_to(depths, xs.shape), np.float64)
+        sl = np.ascontiguousarray(np.broadcast_to(slopes, xs.shape + (2,)), np.float32)
+        ax = np.ascontiguousarray(np.broadcast_to(axes, xs.shape), np.int32)
+        out = np.empty(xs.shape, np.float64)
+        self.lib.pmo_ncc_plane_batch(self._pp, self.sum_i.ctypes.data, self.sum_ii.ctypes.data, xs.size,
+                                     xs.ctypes.data, ys.ctypes.data, vs.ctypes.data, ds.ctypes.data, sl.ctypes.data,
+                                     ax.ctypes.data, out.ctypes.data)
+        return out
+
+    def initial_costs_planes(self, depth: np.ndarray, slopes: np.ndarray) -> np.ndarray:
+        depth = np.ascontiguousarray(depth, np.float64)
+        slopes = np.ascontiguousarray(slopes, np.float32)
+        c = np.empty((self.H, self.W, self.V), np.float64)
+        self.lib.pmo_initial_costs_planes(self._pp, self.sum_i.ctypes.data, self.sum_ii.ctypes.data,
+                                          depth.ctypes.data, slopes.ctypes.data, c.ctypes.data)
+        return c
+
+    def sweep_planes(self, depth: np.ndarray, slopes: np.ndarray, cost: np.ndarray, direction: int, sweep_id: int,
+                     num_samples: int, view_sel: np.ndarray | None = None, lines: tuple[int, int] = (0, -1)) -> int:
+        """In place on float64 depth (H, W), float32 slopes (H, W, 2) and float64 cost (H, W, V)."""
+        assert depth.dtype == np.float64 and depth.flags.c_contiguous
+        assert slopes.dtype == np.float32 and slopes.flags.c_contiguous
+        assert cost.dtype == np.float64 and cost.flags.c_contiguous
+        vs = view_sel.ctypes.data if view_sel is not None else None
+        return self.lib.pmo_sweep_planes(self._pp, self.sum_i.ctypes.data, self.sum_ii.ctypes.data,
+                                         depth.ctypes.data, slopes.ctypes.data, cost.ctypes.data, direction, sweep_id,
+                                         num_samples, vs, lines[0], lines[1])
+
+    def refine_planes(self, depth: np.ndarray, slopes: np.ndarray, view_sel: np.ndarray, num_samples: int,
+                      trials: int, sigma: float, sweep_id: int, axis: int) -> int:
+        assert depth.dtype == np.float64 and depth.flags.c_contiguous
+        slopes = np.ascontiguousarray(slopes, np.float32)
+        vs = np.ascontiguousarray(view_sel, np.uint8)
+        return self.lib.pmo_refine_planes(self._pp, self.sum_i.ctypes.data, self.sum_ii.ctypes.data,
+                                          depth.ctypes.data, slopes.ctypes.data, vs.ctypes.data, num_samples, trials,
+                                          sigma, sweep_id, axis)
+
+    def run_planes(self, iterations: int, num_samples: int):
+        depth = np.empty((self.H, self.W), np.float64)
+        slopes = np.empty((self.H, self.W, 2), np.float32)
+        cost = np.empty((self.H, self.W, self.V), np.float64)
+        vsel = np.full((num_samples, self.H, self.W), 255, np.uint8)
+        n = self.lib.pmo_run_planes(self._pp, iterations, num_samples, self.sum_i.ctypes.data,
+                                    self.sum_ii.ctypes.data, depth.ctypes.data, slopes.ctypes.data, cost.ctypes.data,
+                                    vsel.ctypes.data)
+        return depth, slopes, cost, vsel, n
+
     def run(self, iterations: int, num_samples: int):
         depth = np.empty((self.H, self.W), np.float64)
         cost = np.empty((self.H, self.W, self.V), np.float64)
@@ -242,11 +340,12 @@ def from_images(images, ref_id: int, params, source_texels=None, ref_texels=None
     (as the engine stores them) or derived here (u8/255, then the prefilter)."""
     ref_im = images[ref_id]
     srcs = [im for i, im in enumerate(images) if i != ref_id]
-    hh, ik = [], None
+    hh, ee, ik = [], [], None
     for s in srcs:
         h_, ik = init_relative(ref_im.K, ref_im.R, ref_im.T, s.K, s.R, s.T, params.orientation_x,
                                params.orientation_z)
         hh.append(h_)
+        ee.append(translation_term(ref_im.R, ref_im.T, s.K, s.R, s.T))
 
     def texels(im):
         t = im.image.astype(np.float32) / np.float32(255.0)
@@ -258,6 +357,8 @@ def from_images(images, ref_id: int, params, source_texels=None, ref_texels=None
     src_t = source_texels if source_texels is not None else [texels(s) for s in srcs]
     orc = Oracle(ref_t, src_t, np.array(hh), ik, params.half_window, params.depth_near, params.depth_far,
                  params.sp_alpha, params.seed, (params.orientation_x, 0.0, params.orientation_z),
-                 bool(params.quirks), 0, fp32, getattr(params, "sampler", 0))
+                 bool(params.quirks), 0, fp32, getattr(params, "sampler", 0), np.array(ee))
     orc.p.perturbation = float(getattr(params, "perturbation", 0.0))
+    if getattr(params, "planes", 0):
+        orc.set_planes(True, float(params.plane_depth_step), float(params.plane_slope_step))
     return orc

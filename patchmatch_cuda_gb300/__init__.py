@@ -352,6 +352,36 @@ class Engine:
                                           ds.ctypes.data, ax.ctypes.data, out.ctypes.data))
         return out
 
+    # ---- slanted-plane mode (params.planes = 1) ---------------------------------------------
+    def slopes(self) -> np.ndarray:
+        """Per-pixel plane slopes (a, b), normal ~ (a, b, 1): (height, width, 2) float32."""
+        out = np.empty((self.height, self.width, 2), np.float32)
+        self._chk(self._lib.pm_get_slopes(self.h, out.ctypes.data))
+        return out
+
+    def set_slopes(self, slopes: np.ndarray) -> None:
+        s = np.ascontiguousarray(slopes, np.float32)
+        assert s.shape == (self.height, self.width, 2)
+        self._chk(self._lib.pm_set_slopes(self.h, s.ctypes.data))
+
+    def normals(self) -> np.ndarray:
+        """Unit plane normals in the reference camera: (height, width, 3) float32."""
+        out = np.empty((self.height, self.width, 3), np.float32)
+        self._chk(self._lib.pm_get_normals(self.h, out.ctypes.data))
+        return out
+
+    def eval_costs_planes(self, xs, ys, views, depths, slopes, axes) -> np.ndarray:
+        xs = np.ascontiguousarray(xs, np.int32).ravel()
+        ys = np.ascontiguousarray(np.broadcast_to(ys, xs.shape), np.int32)
+        vs = np.ascontiguousarray(np.broadcast_to(views, xs.shape), np.int32)
+        ds = np.ascontiguousarray(np.broadcast_to(depths, xs.shape), np.float32)
+        sl = np.ascontiguousarray(np.broadcast_to(slopes, xs.shape + (2,)), np.float32)
+        ax = np.ascontiguousarray(np.broadcast_to(axes, xs.shape), np.int32)
+        out = np.empty(xs.shape, np.float32)
+        self._chk(self._lib.pm_eval_costs_planes(self.h, xs.size, xs.ctypes.data, ys.ctypes.data, vs.ctypes.data,
+                                                 ds.ctypes.data, sl.ctypes.data, ax.ctypes.data, out.ctypes.data))
+        return out
+
     def sample_source(self, view: int, xs, ys) -> np.ndarray:
         xs = np.ascontiguousarray(xs, np.float32).ravel()
         ys = np.ascontiguousarray(np.broadcast_to(ys, xs.shape), np.float32)

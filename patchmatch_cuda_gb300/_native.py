@@ -41,7 +41,8 @@ EXPORTED_SYMBOLS = [
     "pm_batch_run", "pm_batch_info", "pm_batch_destroy", "pm_texture_peak", "pm_default_fuse_params",
     "pm_fusion_create", "pm_fusion_create_from_engines", "pm_fusion_run", "pm_fusion_info",
     "pm_fusion_get_points", "pm_fusion_get_depth", "pm_fusion_geometry", "pm_fusion_write_ply",
-    "pm_fusion_last_error", "pm_fusion_destroy", "pm_refine",
+    "pm_fusion_last_error", "pm_fusion_destroy", "pm_refine", "pm_get_slopes", "pm_set_slopes",
+    "pm_get_normals", "pm_eval_costs_planes",
 ]
 
 MAX_FUSE_REFS = 256
@@ -64,7 +65,8 @@ class PmParams(C.Structure):
         ("gpu_id", C.c_int), ("block_dim_x", C.c_int), ("block_dim_y", C.c_int),
         ("sampler", C.c_int), ("texel_format", C.c_int), ("num_sweeps", C.c_int),
         ("proposal_threshold", C.c_float), ("perturbation", C.c_float), ("refine_trials", C.c_int),
-        ("refine_sigma", C.c_float),
+        ("refine_sigma", C.c_float), ("planes", C.c_int), ("plane_depth_step", C.c_float),
+        ("plane_slope_step", C.c_float),
     ]
 
 
@@ -132,6 +134,10 @@ def load_engine() -> C.CDLL:
         "pm_get_ref_maps": (C.c_int, [H, P, P, P]),
         "pm_get_source_texels": (C.c_int, [H, C.c_int, P]),
         "pm_eval_costs": (C.c_int, [H, C.c_int, P, P, P, P, P, P]),
+        "pm_eval_costs_planes": (C.c_int, [H, C.c_int, P, P, P, P, P, P, P]),
+        "pm_get_slopes": (C.c_int, [H, P]),
+        "pm_set_slopes": (C.c_int, [H, P]),
+        "pm_get_normals": (C.c_int, [H, P]),
         "pm_sample_source": (C.c_int, [H, C.c_int, C.c_int, P, P, P]),
         "pm_transpose_layers": (C.c_int, [P, C.c_size_t, P, C.c_size_t, C.c_int, C.c_int, C.c_int, P]),
         "pm_philox": (C.c_int, [C.c_uint64, C.c_int, P, P]),

@@ -26,9 +26,10 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-Wall"]
 
-CUDA_SOURCES = ["pm_win_a.cu", "pm_win_b.cu", "pm_win_c.cu", "pm_win_d.cu", "pm_win_a_hw.cu", "pm_win_b_hw.cu",
-                "pm_win_c_hw.cu", "pm_win_d_hw.cu", "pm_prep.cu", "pm_api.cu", "pm_noalloc.cu", "pm_gemm.cu",
-                "pm_net.cu", "pm_proposal.cu", "pm_fuse.cu"]
+# window-templated kernels: 4 window groups x 2 samplers x 2 plane modes
+WINDOW_SOURCES = [f"pm_win_{g}{hw}{pl}.cu" for pl in ("", "_pl") for hw in ("", "_hw") for g in "dcba"]
+CUDA_SOURCES = WINDOW_SOURCES + ["pm_prep.cu", "pm_api.cu", "pm_noalloc.cu", "pm_gemm.cu", "pm_net.cu",
+                                 "pm_proposal.cu", "pm_fuse.cu"]
 HEADERS = ["pm_device.cuh", "pm_sweep.cuh", "pm_internal.h", "pm_windows.inc"]
 
 

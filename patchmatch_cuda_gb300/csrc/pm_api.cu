@@ -30,6 +30,7 @@ struct pm_handle {
 
     float *d_ref = nullptr, *d_sum_i = nullptr, *d_sum_ii = nullptr, *d_c1 = nullptr;
     float *d_depth = nullptr, *d_cost = nullptr, *d_beta = nullptr;
+    float2 *d_slopes = nullptr;          // slanted-plane mode: per-pixel slopes
     uint8_t *d_view_sel = nullptr;
     unsigned long long *d_evals = nullptr;
     float4 *d_hh = nullptr;
@@ -116,8 +117,9 @@ bool inv3(const double *m, double *o)
 }
 
 // H1 = K_s R_s R_r^T K_r^-1, H2 = K_s R_s (C_s - C_r) n^T K_r^-1 with C = -R^T t.
+// e_out (may be null): e = K_s T_rel, the translation term slanted planes use.
 void relative_homographies(const pm_view &ref, const double *k_ref_inv, const pm_view &src,
-                           double nx, double nz, double out[18])
+                           double nx, double nz, double out[18], double *e_out = nullptr)
 {
     double kr[9], rr[9], tr[3], ks[9], rs[9], ts[3];
     for (int i = 0; i < 9; ++i) { rr[i] = ref.R[i]; ks[i] = src.K[i]; rs[i] = src.R[i]; kr[i] = ref.K[i]; }
@@ -140,6 +142,8 @@ void relative_homographies(const pm_view &ref, const double *k_ref_inv, const pm
     for (int i = 0; i < 9; ++i) out[i] = h1[i];
     for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j) out[9 + 3 * i + j] = kt[i] * nk[j];
+    if (e_out)
+        for (int i = 0; i < 3; ++i) e_out[i] = kt[i];
     (void)kr;
 }
 
@@ -223,6 +227,8 @@ int window_side(const pm_handle *h) { return 2 * h->p.half_window + 1; }
 
 bool hw_of(const pm_handle *h) { return h->p.sampler == PM_SAMPLER_HARDWARE; }
 
+bool pl_of(const pm_handle *h) { return h->p.planes != 0; }
+
 cudaError_t enqueue_costs(pm_handle *h, int axis)
 {
     LaunchReq req{};
@@ -233,7 +239,7 @@ cudaError_t enqueue_costs(pm_handle *h, int axis)
     req.axis = axis;
     const int npix = h->W * h->H;
     req.grid = (npix + COST_BLOCK / 32 - 1) / (COST_BLOCK / 32);
-    return launch_window(window_side(h), h->p.sampler == PM_SAMPLER_HARDWARE, req);
+    return launch_window(window_side(h), hw_of(h), pl_of(h), req);
 }
 
 // Window axis of a sweep direction: 1 for the horizontal sweeps (transposed windows).
@@ -255,7 +261,7 @@ cudaError_t enqueue_refine(const pm_handle *h, const RefDesc *refs, int ref, int
     req.samples = samples;
     const int npix = h->W * h->H;
     req.grid = (npix + COST_BLOCK / 32 - 1) / (COST_BLOCK / 32);
-    return launch_window(window_side(h), h->p.sampler == PM_SAMPLER_HARDWARE, req);
+    return launch_window(window_side(h), hw_of(h), pl_of(h), req);
 }
 
 // The refinement that ends a schedule of `nsweeps` sweeps: on the last sweep's orientation and
@@ -281,12 +287,13 @@ void fill_sweep_args(SweepArgs &a, const RefDesc *refs, const int *lines, int nr
     a.num_samples = num_samples;
     a.record_views = record;
     a.perturb = 0.0f;
+    a.decay = std::exp2(-0.25f * (float)sweep_id);
     a.line_start[0] = 0;
     for (int i = 0; i < nrefs; ++i) a.line_start[i + 1] = a.line_start[i] + lines[i];
     a.total_lines = a.line_start[nrefs];
 }
 
-cudaError_t enqueue_sweep(int win, bool hw, int wpl, const SweepArgs &a, cudaStream_t s)
+cudaError_t enqueue_sweep(int win, bool hw, bool pl, int wpl, const SweepArgs &a, cudaStream_t s)
 {
     if (a.total_lines == 0) return cudaSuccess;
     LaunchReq req{};
@@ -295,7 +302,7 @@ cudaError_t enqueue_sweep(int win, bool hw, int wpl, const SweepArgs &a, cudaStr
     req.sweep = &a;
     req.grid = a.total_lines;
     req.block = 32 * wpl;
-    return launch_window(win, hw, req);
+    return launch_window(win, hw, pl, req);
 }
 
 
@@ -380,7 +387,7 @@ cudaError_t enqueue_schedule(pm_handle *h)
         const int s_first = h->p.init_mode == PM_INIT_RANDOM ? 1 : 0;
         fill_sweep_args(a, h->d_desc, &lines, 1, d, (uint32_t)k, it == 0 ? s_first : 0, k == nsweeps - 1 ? 1 : 0);
         a.perturb = sweep_perturb(h, k);
-        e = enqueue_sweep(window_side(h), hw_of(h), h->wpl[orient(d)], a, h->stream);
+        e = enqueue_sweep(window_side(h), hw_of(h), pl_of(h), h->wpl[orient(d)], a, h->stream);
         if (e != cudaSuccess) return e;
     }
     return enqueue_final_refine(h, h->d_desc, 0, nsweeps, h->p.init_mode == PM_INIT_RANDOM, h->stream);
@@ -418,7 +425,7 @@ cudaError_t tune_warps_per_line(pm_handle *h)
                 float ms = 0.0f;
                 for (int rep = 0; rep < 2; ++rep) {  // first launch warms caches
                     e = cudaEventRecord(h->ev[2], h->stream);
-                    if (e == cudaSuccess) e = enqueue_sweep(h->win, hw_of(h), wpl, a, h->stream);
+                    if (e == cudaSuccess) e = enqueue_sweep(h->win, hw_of(h), pl_of(h), wpl, a, h->stream);
                     if (e == cudaSuccess) e = cudaEventRecord(h->ev[3], h->stream);
                     if (e == cudaSuccess) e = cudaEventSynchronize(h->ev[3]);
                     if (e != cudaSuccess) return e;
@@ -435,7 +442,7 @@ cudaError_t tune_warps_per_line(pm_handle *h)
 }
 
 // Warps per line for a batched launch: the most that still keeps every line resident.
-int batch_wpl(int win, bool hw, int total_lines, int device)
+int batch_wpl(int win, bool hw, bool pl, int total_lines, int device)
 {
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
@@ -445,7 +452,7 @@ int batch_wpl(int win, bool hw, int total_lines, int device)
         r.kind = LaunchKind::SweepOccupancy;
         r.block = 32 * wpl;
         r.occupancy = &occ;
-        if (launch_window(win, hw, r) == cudaSuccess && total_lines <= occ * sms) return wpl;
+        if (launch_window(win, hw, pl, r) == cudaSuccess && total_lines <= occ * sms) return wpl;
     }
     return 1;
 }
@@ -482,6 +489,9 @@ void pm_default_params(pm_params *p)
     p->perturbation = 0.0f;
     p->refine_trials = 0;
     p->refine_sigma = 0.05f;
+    p->planes = 0;
+    p->plane_depth_step = 0.02f;
+    p->plane_slope_step = 0.25f;
     p->threads_per_line = 0;
     p->quirks = 1;
     p->sampler = PM_SAMPLER_HARDWARE;
@@ -511,7 +521,7 @@ pm_status pm_destroy(pm_handle *h)
     }
     if (h->tex_layered) cudaDestroyTextureObject(h->tex_layered);
     if (h->layered) release_array(h->device, h->layer_w, h->layer_h, h->texel_bytes, h->layered, h->V);
-    void *bufs[] = {h->d_ref, h->d_sum_i, h->d_sum_ii, h->d_c1, h->d_depth, h->d_cost, h->d_beta,
+    void *bufs[] = {h->d_ref, h->d_sum_i, h->d_sum_ii, h->d_c1, h->d_depth, h->d_cost, h->d_beta, h->d_slopes,
                     h->d_view_sel, h->d_evals, h->d_hh, h->d_desc, h->d_quarter[0],
                     h->d_quarter[1], h->d_quarter[2], h->d_prop_in, h->d_prop_out};
     for (void *b : bufs)
@@ -549,6 +559,9 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
         !(p.perturbation >= 0.0f && p.perturbation < 1.0f) ||
         p.refine_trials < 0 || p.refine_trials > PM_MAX_REFINE_TRIALS ||
         (p.refine_trials > 0 && !(p.refine_sigma > 0.0f && std::isfinite(p.refine_sigma))) ||
+        (p.planes != 0 && p.planes != 1) ||
+        (p.planes && !(p.plane_depth_step >= 0.0f && p.plane_depth_step < 1.0f)) ||
+        (p.planes && !(p.plane_slope_step >= 0.0f && p.plane_slope_step <= 2.0f)) ||
         (p.sampler != PM_SAMPLER_EXACT && p.sampler != PM_SAMPLER_HARDWARE) ||
         (p.texel_format != PM_TEXELS_AUTO && p.texel_format != PM_TEXELS_U8 &&
          p.texel_format != PM_TEXELS_F16 && p.texel_format != PM_TEXELS_F32) ||
@@ -595,15 +608,20 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
     double kr[9], kr_inv[9];
     for (int i = 0; i < 9; ++i) kr[i] = ref.K[i];
     if (!inv3(kr, kr_inv)) { pm_destroy(h); return PM_ERR_CAMERA; }
-    std::vector<float> hh((size_t)h->V * 20, 0.0f);
+    constexpr int HHF = 4 * HH_F4;  // floats per view: H1, H2, e, padding
+    std::vector<float> hh((size_t)h->V * HHF, 0.0f);
     int si = 0;
     for (int i = 0; i < n_views; ++i) {
         if (i == ref_id) continue;
-        double o[18];
-        relative_homographies(ref, kr_inv, views[i], p.orientation_x, p.orientation_z, o);
+        double o[18], ev[3];
+        relative_homographies(ref, kr_inv, views[i], p.orientation_x, p.orientation_z, o, ev);
         for (int k = 0; k < 18; ++k) {
             if (!std::isfinite(o[k])) { pm_destroy(h); return PM_ERR_CAMERA; }
-            hh[(size_t)si * 20 + k] = (float)o[k];
+            hh[(size_t)si * HHF + k] = (float)o[k];
+        }
+        for (int k = 0; k < 3; ++k) {
+            if (!std::isfinite(ev[k])) { pm_destroy(h); return PM_ERR_CAMERA; }
+            hh[(size_t)si * HHF + 18 + k] = (float)ev[k];
         }
         h->src_w[si] = views[i].width;
         h->src_h[si] = views[i].height;
@@ -680,6 +698,7 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
     PM_TRY(dalloc(&h->d_depth, npix * 4, s));
     PM_TRY(dalloc(&h->d_cost, npix * h->V * 4, s));
     PM_TRY(dalloc(&h->d_beta, npix * h->V * 4, s));
+    if (p.planes) PM_TRY(dalloc(&h->d_slopes, npix * sizeof(float2), s));
     PM_TRY(dalloc(&h->d_view_sel, npix * (size_t)p.num_samples, s));
     PM_TRY(dalloc(&h->d_evals, 2 * sizeof(unsigned long long), s));
     PM_TRY(dalloc(&h->d_hh, hh.size() * 4, s));
@@ -830,6 +849,12 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
     D.nz = p.orientation_z;
     D.ik00 = (float)kr_inv[0];
     D.ik02 = (float)kr_inv[2];
+    D.ik11 = (float)kr_inv[4];
+    D.ik12 = (float)kr_inv[5];
+    D.planes = p.planes;
+    D.plane_dstep = p.plane_depth_step;
+    D.plane_sstep = p.plane_slope_step;
+    D.slopes = h->d_slopes;
     D.quirks = p.quirks ? 1 : 0;
     D.record_sweep = -1;
     D.hw_filter = h->p.sampler == PM_SAMPLER_HARDWARE ? 1 : 0;
@@ -915,7 +940,7 @@ pm_status pm_run(pm_handle *h)
 
 }  // extern "C"
 
-// A batch of references on one device: groups of equal window side and sampler, each with a
+// A batch of references on one device: groups of equal window side, sampler and plane mode, each with a
 // device array of descriptors; every sweep of a group is one launch over the lines of all of
 // its references.
 struct pm_batch {
@@ -924,6 +949,7 @@ struct pm_batch {
         RefDesc *d_descs = nullptr;
         int win = 0;
         bool hw = false;
+        bool pl = false;      // slanted planes
         int wpl[2] = {0, 0};  // warps per line: vertical, horizontal sweeps (0: occupancy rule)
     };
     std::vector<pm_handle *> hs;
@@ -956,7 +982,7 @@ cudaError_t enqueue_batch(pm_batch *b, cudaStream_t s)
             req.ref_index = i;
             req.axis = 1;
             req.grid = (h->W * h->H + COST_BLOCK / 32 - 1) / (COST_BLOCK / 32);
-            e = launch_window(h->win, hw_of(h), req);
+            e = launch_window(h->win, hw_of(h), pl_of(h), req);
             if (e != cudaSuccess) return e;
             b->launches += 2;
             max_sweeps = std::max(max_sweeps, schedule_sweeps(h));
@@ -973,8 +999,9 @@ cudaError_t enqueue_batch(pm_batch *b, cudaStream_t s)
             const int s_first = g.refs[0]->p.init_mode == PM_INIT_RANDOM ? 1 : 0;
             fill_sweep_args(a, g.d_descs, lines.data(), m, d, (uint32_t)k, it == 0 ? s_first : 0, 1);
             a.perturb = sweep_perturb(g.refs[0], k);
-            const int wpl = g.wpl[orient(d)] ? g.wpl[orient(d)] : batch_wpl(g.win, g.hw, a.total_lines, b->hs[0]->device);
-            const cudaError_t e = enqueue_sweep(g.win, g.hw, wpl, a, s);
+            const int wpl = g.wpl[orient(d)] ? g.wpl[orient(d)]
+                                              : batch_wpl(g.win, g.hw, g.pl, a.total_lines, b->hs[0]->device);
+            const cudaError_t e = enqueue_sweep(g.win, g.hw, g.pl, wpl, a, s);
             if (e != cudaSuccess) return e;
             ++b->launches;
         }
@@ -1009,7 +1036,7 @@ cudaError_t tune_batch(pm_batch *b, cudaEvent_t e0, cudaEvent_t e1)
             req.ref_index = i;
             req.axis = 1;
             req.grid = (h->W * h->H + COST_BLOCK / 32 - 1) / (COST_BLOCK / 32);
-            if (e == cudaSuccess) e = launch_window(h->win, hw_of(h), req);
+            if (e == cudaSuccess) e = launch_window(h->win, hw_of(h), pl_of(h), req);
         }
         if (e != cudaSuccess) return e;
         for (int o = 0; o < 2; ++o) {
@@ -1023,7 +1050,7 @@ cudaError_t tune_batch(pm_batch *b, cudaEvent_t e0, cudaEvent_t e1)
                 float ms = 0.0f;
                 for (int rep = 0; rep < 2; ++rep) {  // the first launch warms the caches
                     e = cudaEventRecord(e0, s);
-                    if (e == cudaSuccess) e = enqueue_sweep(g.win, g.hw, wpl, a, s);
+                    if (e == cudaSuccess) e = enqueue_sweep(g.win, g.hw, g.pl, wpl, a, s);
                     if (e == cudaSuccess) e = cudaEventRecord(e1, s);
                     if (e == cudaSuccess) e = cudaEventSynchronize(e1);
                     if (e != cudaSuccess) return e;
@@ -1057,7 +1084,8 @@ pm_status batch_setup(pm_handle *const *hs, int n, pm_batch *b)
         if (done[g0]) continue;
         std::vector<pm_handle *> grp;
         for (int i = g0; i < n; ++i)
-            if (!done[i] && hs[i]->win == hs[g0]->win && hw_of(hs[i]) == hw_of(hs[g0])) {
+            if (!done[i] && hs[i]->win == hs[g0]->win && hw_of(hs[i]) == hw_of(hs[g0]) &&
+                pl_of(hs[i]) == pl_of(hs[g0])) {
                 grp.push_back(hs[i]);
                 done[i] = 1;
             }
@@ -1066,6 +1094,7 @@ pm_status batch_setup(pm_handle *const *hs, int n, pm_batch *b)
             g.refs.assign(grp.begin() + start, grp.begin() + std::min(grp.size(), start + MAX_BATCH_REFS));
             g.win = grp[0]->win;
             g.hw = hw_of(grp[0]);
+            g.pl = pl_of(grp[0]);
             PM_CUDA(hs[0], cudaMalloc((void **)&g.d_descs, sizeof(RefDesc) * g.refs.size()));
             for (size_t i = 0; i < g.refs.size(); ++i) {
                 // each reference records the views of its own last sweep only, as a single run does
@@ -1316,7 +1345,7 @@ pm_status pm_run_sweep(pm_handle *h, int direction, uint32_t sweep_id, int num_s
         PM_CUDA(h, cudaMemcpyAsync(h->d_cost, c.data(), c.size() * 4, cudaMemcpyHostToDevice, h->stream));
     }
     PM_CUDA(h, cudaEventRecord(h->ev[2], h->stream));
-    PM_CUDA(h, enqueue_sweep(h->win, hw_of(h), h->wpl[orient(direction)], a, h->stream));
+    PM_CUDA(h, enqueue_sweep(h->win, hw_of(h), pl_of(h), h->wpl[orient(direction)], a, h->stream));
     PM_CUDA(h, cudaEventRecord(h->ev[3], h->stream));
     PM_CUDA(h, cudaStreamSynchronize(h->stream));
     float ms = 0.0f;
@@ -1433,8 +1462,30 @@ pm_status pm_get_source_texels(pm_handle *h, int view, float *dst)
     return PM_OK;
 }
 
+namespace {
+pm_status eval_costs(pm_handle *h, int n, const int *xs, const int *ys, const int *views, const float *depths,
+                     const float *slopes, const int *axes, float *out);
+}
+
 pm_status pm_eval_costs(pm_handle *h, int n, const int *xs, const int *ys, const int *views,
                         const float *depths, const int *axes, float *out)
+{
+    return eval_costs(h, n, xs, ys, views, depths, nullptr, axes, out);
+}
+
+pm_status pm_eval_costs_planes(pm_handle *h, int n, const int *xs, const int *ys, const int *views,
+                               const float *depths, const float *slopes, const int *axes, float *out)
+{
+    if (h && !h->d_slopes) return fail(h, PM_ERR_STATE, "the handle was created without slanted planes");
+    if (n > 0 && !slopes) return PM_ERR_INVALID_ARGUMENT;
+    return eval_costs(h, n, xs, ys, views, depths, slopes, axes, out);
+}
+
+}  // extern "C"
+
+namespace {
+pm_status eval_costs(pm_handle *h, int n, const int *xs, const int *ys, const int *views, const float *depths,
+                     const float *slopes, const int *axes, float *out)
 {
     if (!h || n < 0 || (n > 0 && (!xs || !ys || !views || !depths || !axes || !out)))
         return PM_ERR_INVALID_ARGUMENT;
@@ -1450,12 +1501,15 @@ pm_status pm_eval_costs(pm_handle *h, int n, const int *xs, const int *ys, const
     if (st != PM_OK) return st;
     int4 *d_q = nullptr;
     float *d_d = nullptr, *d_o = nullptr;
+    float2 *d_s = nullptr;
     cudaStream_t s = h->stream;
     PM_CUDA(h, cudaMallocAsync((void **)&d_q, sizeof(int4) * n, s));
     PM_CUDA(h, cudaMallocAsync((void **)&d_d, sizeof(float) * n, s));
     PM_CUDA(h, cudaMallocAsync((void **)&d_o, sizeof(float) * n, s));
+    if (slopes) PM_CUDA(h, cudaMallocAsync((void **)&d_s, sizeof(float2) * n, s));
     PM_CUDA(h, cudaMemcpyAsync(d_q, q.data(), sizeof(int4) * n, cudaMemcpyHostToDevice, s));
     PM_CUDA(h, cudaMemcpyAsync(d_d, depths, sizeof(float) * n, cudaMemcpyHostToDevice, s));
+    if (slopes) PM_CUDA(h, cudaMemcpyAsync(d_s, slopes, sizeof(float2) * n, cudaMemcpyHostToDevice, s));
     LaunchReq req{};
     req.kind = LaunchKind::Eval;
     req.stream = s;
@@ -1464,14 +1518,61 @@ pm_status pm_eval_costs(pm_handle *h, int n, const int *xs, const int *ys, const
     req.n = n;
     req.queries = d_q;
     req.depths = d_d;
+    req.slopes = d_s;
     req.out = d_o;
     req.grid = std::min((n + COST_BLOCK / 32 - 1) / (COST_BLOCK / 32), 65535);
-    PM_CUDA(h, launch_window(h->win, hw_of(h), req));
+    PM_CUDA(h, launch_window(h->win, hw_of(h), pl_of(h), req));
     PM_CUDA(h, cudaMemcpyAsync(out, d_o, sizeof(float) * n, cudaMemcpyDeviceToHost, s));
     PM_CUDA(h, cudaFreeAsync(d_q, s));
     PM_CUDA(h, cudaFreeAsync(d_d, s));
     PM_CUDA(h, cudaFreeAsync(d_o, s));
+    if (d_s) PM_CUDA(h, cudaFreeAsync(d_s, s));
     PM_CUDA(h, cudaStreamSynchronize(s));
+    return PM_OK;
+}
+}  // namespace
+
+extern "C" {
+
+pm_status pm_get_slopes(pm_handle *h, float *dst)
+{
+    if (!h || !dst) return PM_ERR_INVALID_ARGUMENT;
+    if (!h->d_slopes) return fail(h, PM_ERR_STATE, "the handle was created without slanted planes");
+    pm_status st = set_device(h);
+    if (st != PM_OK) return st;
+    PM_CUDA(h, cudaMemcpyAsync(dst, h->d_slopes, (size_t)h->W * h->H * sizeof(float2), cudaMemcpyDeviceToHost,
+                               h->stream));
+    PM_CUDA(h, cudaStreamSynchronize(h->stream));
+    return PM_OK;
+}
+
+pm_status pm_set_slopes(pm_handle *h, const float *src)
+{
+    if (!h || !src) return PM_ERR_INVALID_ARGUMENT;
+    if (!h->d_slopes) return fail(h, PM_ERR_STATE, "the handle was created without slanted planes");
+    const size_t n = (size_t)h->W * h->H * 2;
+    for (size_t i = 0; i < n; ++i)
+        if (!std::isfinite(src[i])) return fail(h, PM_ERR_INVALID_ARGUMENT, "slopes must be finite");
+    pm_status st = set_device(h);
+    if (st != PM_OK) return st;
+    PM_CUDA(h, cudaMemcpyAsync(h->d_slopes, src, n * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+    PM_CUDA(h, cudaStreamSynchronize(h->stream));
+    return PM_OK;
+}
+
+pm_status pm_get_normals(pm_handle *h, float *dst)
+{
+    if (!h || !dst) return PM_ERR_INVALID_ARGUMENT;
+    std::vector<float> sl((size_t)h->W * h->H * 2);
+    pm_status st = pm_get_slopes(h, sl.data());
+    if (st != PM_OK) return st;
+    for (size_t i = 0; i < (size_t)h->W * h->H; ++i) {
+        const double a = sl[2 * i], b = sl[2 * i + 1];
+        const double inv = 1.0 / std::sqrt(a * a + b * b + 1.0);
+        dst[3 * i] = (float)(a * inv);
+        dst[3 * i + 1] = (float)(b * inv);
+        dst[3 * i + 2] = (float)inv;
+    }
     return PM_OK;
 }
 

@@ -262,6 +262,10 @@ int main(int argc, char **argv)
     if (has("prefilter")) p.prefilter = std::atoi(get("prefilter").c_str());
     if (has("seed")) p.seed = std::strtoull(get("seed").c_str(), nullptr, 10);
     if (has("precision")) p.precision = std::atoi(get("precision").c_str());
+    // the engine's own keys (no counterpart in the reference's INI): slanted planes per pixel
+    if (has("planes")) p.planes = std::atoi(get("planes").c_str());
+    if (has("planeDepthStep")) p.plane_depth_step = std::strtof(get("planeDepthStep").c_str(), nullptr);
+    if (has("planeSlopeStep")) p.plane_slope_step = std::strtof(get("planeSlopeStep").c_str(), nullptr);
     const std::string out = get("outputFileName");
 
     const std::string list = get("imageInfoFileName");

@@ -25,6 +25,24 @@ enum : uint32_t {
 };
 constexpr uint32_t INIT_SWEEP_ID = 0xFFFFFFFFu;
 
+// Per-view homography table entries (float4): H1 (floats 0-8), H2 (9-17) for the one plane
+// normal of the reference, e = K_s T_rel (18-20) for per-pixel planes, padding (21-23).
+constexpr int HH_F4 = 6;
+
+// Slanted-plane mode (no counterpart in the reference, whose plane normal is one constant,
+// patchMatch.cu:32): a pixel's plane is its depth d and slopes (a, b), normal n ~ (a, b, 1) in
+// the reference camera, so n . X = d s with the plane scale s = g . (x + 1/2, y + 1/2, 1),
+// g = (a ik00, b ik11, a ik02 + b ik12 + 1), floored at SCALE_MIN; the homography is
+// H1 - e g^T / (d s). Random slopes are uniform in [-SLOPE_DRAW, SLOPE_DRAW]^2, perturbed
+// slopes clamp to [-SLOPE_MAX, SLOPE_MAX].
+constexpr float SLOPE_DRAW = 1.0f;
+constexpr float SLOPE_MAX = 2.0f;
+constexpr float SCALE_MIN = 0.0625f;
+// The random hypothesis's kind from its counter's second word u: u < 1/3 a uniform depth with
+// the current slopes, u < 2/3 the current depth with uniform slopes, else a local perturbation.
+constexpr float PLANE_P_DEPTH = 0.33333334f;
+constexpr float PLANE_P_SLOPE = 0.6666667f;
+
 // Transition probabilities and the uniform-emission cost of the HMM, as float constants
 // (FIX_STATE_PROB 0.999f and CHANGE_STATE_PROB = 1.0f - 0.999f).
 constexpr float FIX_STATE_PROB = 0.999f;
@@ -38,6 +56,9 @@ struct RefDesc {
     float a2;                       // SPMAlpha^2 (float product)
     float u_emit;                   // exp(-0.83^2 / (2 a2))
     float nx, nz, ik00, ik02;       // plane scale s = nx (ik00 (x+1/2) + ik02) + nz
+    float ik11, ik12;               // K^-1 (1,1), (1,2): slanted-plane mode
+    int planes;                     // 1: a slanted plane per pixel (slopes); 0: one normal
+    float plane_dstep, plane_sstep; // slanted planes: local search half-widths at sweep 0
     int quirks;
     int hw_filter;                  // textures filter bilinearly in hardware
     int record_sweep;               // >= 0: views are recorded only in this sweep (batches,
@@ -53,8 +74,9 @@ struct RefDesc {
     float *cost;                    // height*width*n_src, pixel-major
     float *beta;                    // scratch: width*height*n_src backward messages
     uint8_t *view_sel;              // num_samples*height*width or null
+    float2 *slopes;                 // height*width plane slopes (a, b); slanted-plane mode
     unsigned long long *evals;      // [0] algorithmic count, [1] computed count
-    const float4 *hh;               // n_src * 5 float4: H1 (9), H2 (9), pad (2)
+    const float4 *hh;               // n_src * HH_F4 float4: H1 (9), H2 (9), e (3), pad (3)
     cudaTextureObject_t tex_layered;  // all sources as layers (texture-filtering sampler)
     cudaTextureObject_t tex[MAX_VIEWS];
     float src_w[MAX_VIEWS], src_h[MAX_VIEWS];
@@ -281,6 +303,7 @@ __device__ __forceinline__ void load_window(const RefDesc &D, int x, int y, int 
     if (lane == 0) {
         wc.ox = (float)x0 + 0.5f;
         wc.oy = (float)y0 + 0.5f;
+
         // explicit IEEE operations: the texture-filtering sampler's coordinates are
         // replicated bit for bit by the oracle
         wc.scale = __fadd_rn(__fmul_rn(D.nx, fmaf(D.ik00, __fadd_rn((float)x, 0.5f), D.ik02)), D.nz);
@@ -297,26 +320,59 @@ __device__ __forceinline__ void load_window(const RefDesc &D, int x, int y, int 
     }
 }
 
-// Plane-induced homography of (view, depth): T = H1 - H2 / (depth * scale)
-// (patchMatch.cu:462-474); its first two columns and T (ox, oy, 1) at the window origin.
+// A homography's first two columns and its value at the window origin (see warp_setup).
 struct WarpSetup {
     float c0x, c0y, c0z, c1x, c1y, c1z, bx, by, bz;
 };
 
-template <bool HW>
-__device__ __forceinline__ WarpSetup warp_setup(const float4 *hh, int view, float depth,
-                                                float scale, float ox, float oy)
+// g = K_r^-T n for n = (a, b, 1) and the plane scale at pixel centre (px, py), with explicit
+// single-precision steps (the oracle repeats them bit for bit).
+struct PlaneG {
+    float g0, g1, g2, s;
+};
+
+__device__ __forceinline__ PlaneG plane_terms(const RefDesc &D, float2 sl, float px, float py)
 {
-    const float4 *h = hh + 5 * view;
-    const float4 a = h[0], b = h[1], c = h[2], d = h[3], e = h[4];
-    // 20 floats per view: H1 (row-major, floats 0-8), H2 (floats 9-17), 2 pad.
+    PlaneG r;
+    r.g0 = __fmul_rn(sl.x, D.ik00);
+    r.g1 = __fmul_rn(sl.y, D.ik11);
+    r.g2 = fmaf(sl.x, D.ik02, fmaf(sl.y, D.ik12, 1.0f));
+    const float s = fmaf(r.g0, px, fmaf(r.g1, py, r.g2));
+    r.s = s < SCALE_MIN ? SCALE_MIN : s;
+    return r;
+}
+
+// Plane-induced homography of (view, depth): T = H1 - H2 / (depth * scale)
+// (patchMatch.cu:462-474), or with per-pixel planes T = H1 - e g^T / (depth * s); its first two
+// columns and T (ox, oy, 1) at the window origin.
+template <bool HW, bool PL>
+__device__ __forceinline__ WarpSetup warp_setup(const RefDesc &D, const float4 *hh, int view, float depth,
+                                                float2 sl, float scale, float ox, float oy, float hwf)
+{
+    const float4 *h = hh + HH_F4 * view;
+    const float4 a = h[0], b = h[1], c = h[2];
+    // floats 0-8: H1 (row-major), 9-17: H2, 18-20: e
     const float h1[9] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x};
-    const float h2[9] = {c.y, c.z, c.w, d.x, d.y, d.z, d.w, e.x, e.y};
-    // texture-filtering sampler: correctly rounded, so the oracle reproduces the coordinates
-    const float s = HW ? rcp_nr(__fmul_rn(depth, scale)) : __fdividef(1.0f, depth * scale);
     float t[9];
+    if (PL) {
+        const float4 e4 = h[4], e5 = h[5];
+        const float e[3] = {e4.z, e4.w, e5.x};
+        // the pixel centre x + 1/2 = ox + half-window, exactly
+        const PlaneG G = plane_terms(D, sl, ox + hwf, oy + hwf);
+        const float g[3] = {G.g0, G.g1, G.g2};
+        const float s = HW ? rcp_nr(__fmul_rn(depth, G.s)) : __fdividef(1.0f, depth * G.s);
 #pragma unroll
-    for (int i = 0; i < 9; ++i) t[i] = fmaf(-s, h2[i], h1[i]);
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) t[3 * r + k] = fmaf(-s, __fmul_rn(e[r], g[k]), h1[3 * r + k]);
+    } else {
+        const float4 d = h[3], e = h[4];
+        const float h2[9] = {c.y, c.z, c.w, d.x, d.y, d.z, d.w, e.x, e.y};
+        // texture-filtering sampler: correctly rounded, so the oracle reproduces the coordinates
+        const float s = HW ? rcp_nr(__fmul_rn(depth, scale)) : __fdividef(1.0f, depth * scale);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) t[i] = fmaf(-s, h2[i], h1[i]);
+    }
     if (HW) {
         // texture coordinates are (u/z + 1/2, v/z + 1/2): add z/2 to the first two rows
 #pragma unroll
@@ -377,8 +433,9 @@ __device__ __forceinline__ void column_moments(const WarpSetup &A, cudaTextureOb
             j = fetch<HW>(tex, layer, sw, sh, fmaf(A.c1x, fdy, colx), fmaf(A.c1y, fdy, coly),
                           fmaf(A.c1z, fdy, colz));
         const float b = tab[dy * W + cc];
-        // the shift: row 0's sample (fetched whatever its row's bounds; any finite value works)
-        if (dy == 0) m.k = j;
+        // the shift: the sample of the first row inside the reference image (row 0 of a full
+        // window), so that K = 0 and s2 = 0 say exactly that every in-bounds sample is zero
+        if (FULL ? dy == 0 : dy == wc.dy_lo) m.k = j;
         // lanes off the window's columns fetch nothing: j = K = 0 there
         const float d = (FULL || (dy >= wc.dy_lo && dy <= wc.dy_hi)) ? j - m.k : 0.0f;
         m.s1 += d;
@@ -421,15 +478,17 @@ __device__ __forceinline__ float ncc_finalize(bool all_zero, float c2, float x, 
 // Two windowed NCC evaluations of one pixel, (view va, depth da) and (vb, db); every lane
 // receives both results. hh: the homography table (D.hh or a shared-memory copy). FULL: the
 // window lies inside the reference image.
-template <int W, bool HW, bool FULL>
+template <int W, bool HW, bool FULL, bool PL>
 __device__ __forceinline__ void ncc_pair_core(const RefDesc &D, const float4 *hh, const WinCtl &wc,
                                               const float *tab, const float *col, int lane, int va,
-                                              float da, int vb, float db, float &ra, float &rb)
+                                              float da, float2 sa, int vb, float db, float2 sb, float &ra,
+                                              float &rb)
 {
     if (Window<W>::HALF) {
         const int half = lane >> 4, c = lane & 15;
         const int v = half ? vb : va;
-        const WarpSetup A = warp_setup<HW>(hh, v, half ? db : da, wc.scale, wc.ox, wc.oy);
+        const WarpSetup A = warp_setup<HW, PL>(D, hh, v, half ? db : da, half ? sb : sa, wc.scale, wc.ox, wc.oy,
+                                                   (float)Window<W>::HW);
         const cudaTextureObject_t tex = HW ? D.tex_layered : D.tex[v];
         const bool col_ok = c < W && (FULL || (unsigned)(wc.x0 + c) < (unsigned)D.width);
         ColMoments m;
@@ -458,13 +517,14 @@ __device__ __forceinline__ void ncc_pair_core(const RefDesc &D, const float4 *hh
         constexpr int COLS = Window<W>::COLS;
         const int vv[2] = {va, vb};
         const float dd[2] = {da, db};
+        const float2 ss[2] = {sa, sb};
         const float rows = FULL ? (float)W : wc.rows;
         const float inv_rows = FULL ? 1.0f / (float)W : wc.inv_rows;
         float out[2];
 #pragma unroll
         for (int e = 0; e < 2; ++e) {
             const int v = vv[e];
-            const WarpSetup A = warp_setup<HW>(hh, v, dd[e], wc.scale, wc.ox, wc.oy);
+            const WarpSetup A = warp_setup<HW, PL>(D, hh, v, dd[e], ss[e], wc.scale, wc.ox, wc.oy, (float)Window<W>::HW);
             const cudaTextureObject_t tex = HW ? D.tex_layered : D.tex[v];
             ColMoments m[COLS];
             bool ok[COLS];
@@ -500,21 +560,24 @@ __device__ __forceinline__ void ncc_pair_core(const RefDesc &D, const float4 *hh
 }
 
 // Windows cut by the image border: out of line, so the hot loop stays small.
-template <int W, bool HW>
+template <int W, bool HW, bool PL>
 __device__ __noinline__ void ncc_pair_edge(const RefDesc &D, const float4 *hh, const WinCtl &wc,
                                            const float *tab, const float *col, int lane, int va,
-                                           float da, int vb, float db, float &ra, float &rb)
+                                           float da, float2 sa, int vb, float db, float2 sb, float &ra,
+                                           float &rb)
 {
-    ncc_pair_core<W, HW, false>(D, hh, wc, tab, col, lane, va, da, vb, db, ra, rb);
+    ncc_pair_core<W, HW, false, PL>(D, hh, wc, tab, col, lane, va, da, sa, vb, db, sb, ra, rb);
 }
 
-template <int W, bool HW>
+// PL: slanted-plane mode; sa, sb are then the hypotheses' plane slopes (ignored otherwise).
+template <int W, bool HW, bool PL>
 __device__ __forceinline__ void ncc_pair(const RefDesc &D, const float4 *hh, const WinCtl &wc,
                                          const float *tab, const float *col, int lane, int va,
-                                         float da, int vb, float db, float &ra, float &rb)
+                                         float da, float2 sa, int vb, float db, float2 sb, float &ra,
+                                         float &rb)
 {
-    if (wc.full) ncc_pair_core<W, HW, true>(D, hh, wc, tab, col, lane, va, da, vb, db, ra, rb);
-    else ncc_pair_edge<W, HW>(D, hh, wc, tab, col, lane, va, da, vb, db, ra, rb);
+    if (wc.full) ncc_pair_core<W, HW, true, PL>(D, hh, wc, tab, col, lane, va, da, sa, vb, db, sb, ra, rb);
+    else ncc_pair_edge<W, HW, PL>(D, hh, wc, tab, col, lane, va, da, sa, vb, db, sb, ra, rb);
 }
 
 // Copies a reference's descriptor and homography table into shared memory (all threads of
@@ -527,7 +590,7 @@ __device__ __forceinline__ void stage_ref(const RefDesc &src, RefDesc &dst, floa
     uint32_t *d = reinterpret_cast<uint32_t *>(&dst);
     for (int i = threadIdx.x; i < (int)(sizeof(RefDesc) / 4); i += blockDim.x) d[i] = s[i];
     const float4 *h = src.hh;
-    const int n = 5 * src.n_src;
+    const int n = HH_F4 * src.n_src;
     for (int i = threadIdx.x; i < n; i += blockDim.x) hh[i] = __ldg(h + i);
 }
 

@@ -26,6 +26,7 @@ struct LaunchReq {
     int n;
     const int4 *queries;
     const float *depths;
+    const float2 *slopes;      // Eval: per-query plane slopes, or null
     float *out;
     // Refine (axis, refs, ref_index as Costs)
     int trials;
@@ -34,30 +35,31 @@ struct LaunchReq {
     int samples;
 };
 
-// Window-size and sampler dispatch, split over translation units so they compile in
-// parallel. Each returns cudaErrorInvalidValue when W is not in its group. The _hw groups
-// sample through texture-unit bilinear filtering, the others through exact gathers.
-cudaError_t launch_group_a(int W, const LaunchReq &req);     // 3 .. 11
-cudaError_t launch_group_b(int W, const LaunchReq &req);     // 13 .. 17
-cudaError_t launch_group_c(int W, const LaunchReq &req);     // 19 .. 25
-cudaError_t launch_group_d(int W, const LaunchReq &req);     // 27 .. 45
-cudaError_t launch_group_a_hw(int W, const LaunchReq &req);
-cudaError_t launch_group_b_hw(int W, const LaunchReq &req);
-cudaError_t launch_group_c_hw(int W, const LaunchReq &req);
-cudaError_t launch_group_d_hw(int W, const LaunchReq &req);
+// Window-size, sampler and plane-mode dispatch, split over translation units so they compile
+// in parallel. Each returns cudaErrorInvalidValue when W is not in its group. The _hw groups
+// sample through texture-unit bilinear filtering, the others through exact gathers; the _pl
+// groups hold the slanted-plane kernels.
+#define PM_DECLARE_GROUPS(g)                                          \
+    cudaError_t launch_group_##g(int W, const LaunchReq &req);        \
+    cudaError_t launch_group_##g##_hw(int W, const LaunchReq &req);   \
+    cudaError_t launch_group_##g##_pl(int W, const LaunchReq &req);   \
+    cudaError_t launch_group_##g##_hw_pl(int W, const LaunchReq &req);
+PM_DECLARE_GROUPS(a)  // 3 .. 11
+PM_DECLARE_GROUPS(b)  // 13 .. 17
+PM_DECLARE_GROUPS(c)  // 19 .. 25
+PM_DECLARE_GROUPS(d)  // 27 .. 45
+#undef PM_DECLARE_GROUPS
 
-inline cudaError_t launch_window(int W, bool hw, const LaunchReq &req)
+inline cudaError_t launch_window(int W, bool hw, bool pl, const LaunchReq &req)
 {
-    if (hw) {
-        if (W <= 11) return launch_group_a_hw(W, req);
-        if (W <= 17) return launch_group_b_hw(W, req);
-        if (W <= 25) return launch_group_c_hw(W, req);
-        return launch_group_d_hw(W, req);
-    }
-    if (W <= 11) return launch_group_a(W, req);
-    if (W <= 17) return launch_group_b(W, req);
-    if (W <= 25) return launch_group_c(W, req);
-    return launch_group_d(W, req);
+#define PM_PICK(g)                                                                      \
+    return hw ? (pl ? launch_group_##g##_hw_pl(W, req) : launch_group_##g##_hw(W, req)) \
+              : (pl ? launch_group_##g##_pl(W, req) : launch_group_##g(W, req));
+    if (W <= 11) PM_PICK(a)
+    if (W <= 17) PM_PICK(b)
+    if (W <= 25) PM_PICK(c)
+    PM_PICK(d)
+#undef PM_PICK
 }
 
 // Prefilter, moments, conversions, init, transpose, Philox (pm_prep.cu).

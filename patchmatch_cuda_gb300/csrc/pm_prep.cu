@@ -92,8 +92,12 @@ __global__ void init_depth_kernel(const RefDesc *refs, int r, int npix)
     const RefDesc &D = refs[r];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= npix) return;
-    const float u = draw_uniform(D.seed, (uint32_t)i, INIT_SWEEP_ID, RNG_INIT, 0, D.batch_id);
-    D.depth[i] = fmaf(1.0f - u, D.depth_span, D.depth_near);
+    const float4 u = draw_uniform4(D.seed, (uint32_t)i, INIT_SWEEP_ID, RNG_INIT, 0, D.batch_id);
+    D.depth[i] = fmaf(1.0f - u.x, D.depth_span, D.depth_near);
+    // slanted planes: slopes uniform in [-SLOPE_DRAW, SLOPE_DRAW]^2 from the same counter
+    if (D.planes)
+        D.slopes[i] = make_float2(__fmul_rn(SLOPE_DRAW, fmaf(2.0f, u.y, -1.0f)),
+                                  __fmul_rn(SLOPE_DRAW, fmaf(2.0f, u.z, -1.0f)));
 }
 
 __global__ void sample_kernel(const RefDesc *refs, int r, int view, int n,

@@ -104,14 +104,18 @@ __global__ void proposal_init_kernel(const RefDesc *refs, int r, ProposalGeom g,
             c += wy[a] * wx[b] * q[1];
         }
     float depth;
+    float2 sl = make_float2(0.0f, 0.0f);  // slanted planes: fronto-parallel where predicted
     if (c >= threshold) {
         depth = 1.0f / (g.inv_far + s * g.inv_range);
         depth = fminf(fmaxf(depth, D.depth_near), D.depth_near + D.depth_span);
     } else {
-        const float u = draw_uniform(D.seed, (uint32_t)i, INIT_SWEEP_ID, RNG_INIT, 0, D.batch_id);
-        depth = fmaf(1.0f - u, D.depth_span, D.depth_near);
+        // the random initialisation (init_depth_kernel), slopes included
+        const float4 u = draw_uniform4(D.seed, (uint32_t)i, INIT_SWEEP_ID, RNG_INIT, 0, D.batch_id);
+        depth = fmaf(1.0f - u.x, D.depth_span, D.depth_near);
+        sl = make_float2(__fmul_rn(SLOPE_DRAW, fmaf(2.0f, u.y, -1.0f)), __fmul_rn(SLOPE_DRAW, fmaf(2.0f, u.z, -1.0f)));
     }
     D.depth[i] = depth;
+    if (D.planes) D.slopes[i] = sl;
 }
 
 }  // namespace

@@ -31,6 +31,7 @@ struct SweepArgs {
     int num_samples;                     // > 0 overrides the descriptors' (iteration 0: 1)
     int record_views;
     float perturb;                       // > 0: local random search of half-width perturb
+    float decay;                         // 2^(-sweep/4): scales the slanted-plane search widths
     int line_start[MAX_BATCH_REFS + 1];  // prefix sums of lines per reference
 };
 
@@ -58,6 +59,7 @@ struct StepCtl {
     int tested;              // samples that found a view
     float c1sum;             // sum of the drawn views' current costs, in draw order
     float d_former, d_rand, d_cur;
+    float2 sl_f, sl_c, sl_r;  // slanted-plane mode: slopes of the three hypotheses
     int8_t sel[MAX_VIEWS];   // view of each draw, -1 when the CDF found none
 };
 
@@ -67,6 +69,7 @@ struct StepDraws {
     float sample[MAX_VIEWS];  // view samples (RNG_SAMPLE)
     float depth;              // random depth (RNG_RAND_DEPTH, first word)
     float mode;               // local or global random search (RNG_RAND_DEPTH, second word)
+    float sa, sb;             // slanted planes: random slopes (RNG_RAND_DEPTH, words 3 and 4)
 };
 
 __device__ __forceinline__ void make_draws(const RefDesc &D, uint32_t pix, uint32_t sweep, int S,
@@ -77,19 +80,23 @@ __device__ __forceinline__ void make_draws(const RefDesc &D, uint32_t pix, uint3
     // lanes below S draw the view samples; the last lane the random depth (when S < 32)
     const bool depth_lane = lane == 31 && S < 32;
     if (lane < S || depth_lane) {
-        const float2 u = draw_uniform2(seed, pix, sweep, depth_lane ? RNG_RAND_DEPTH : RNG_SAMPLE,
+        const float4 u = draw_uniform4(seed, pix, sweep, depth_lane ? RNG_RAND_DEPTH : RNG_SAMPLE,
                                        depth_lane ? 0 : lane, batch);
         if (depth_lane) {
             out.depth = u.x;
             out.mode = u.y;
+            out.sa = u.z;
+            out.sb = u.w;
         } else {
             out.sample[lane] = u.x;
         }
     }
     if (S >= 32 && lane == 0) {
-        const float2 u = draw_uniform2(seed, pix, sweep, RNG_RAND_DEPTH, 0, batch);
+        const float4 u = draw_uniform4(seed, pix, sweep, RNG_RAND_DEPTH, 0, batch);
         out.depth = u.x;
         out.mode = u.y;
+        out.sa = u.z;
+        out.sb = u.w;
     }
 }
 
@@ -104,7 +111,7 @@ __device__ __forceinline__ void make_draws(const RefDesc &D, uint32_t pix, uint3
 //   B2 .. B3   every warp forms the same argmin; unless the current depth won, the other
 //              views' NCCs at the chosen depth, two views per pass;
 //   after B3   warp 0 commits the costs, the depth and the forward message.
-template <int W, bool HW>
+template <int W, bool HW, bool PL>
 __global__ void __maxnreg__(SweepRegs<HW>::value) sweep_kernel(const __grid_constant__ SweepArgs A)
 {
     constexpr int TAB = Window<W>::TAB;
@@ -114,7 +121,7 @@ __global__ void __maxnreg__(SweepRegs<HW>::value) sweep_kernel(const __grid_cons
     const int gline = blockIdx.x;
     const int r = find_ref(A, gline);
     __shared__ RefDesc D;
-    __shared__ float4 s_hh[5 * MAX_VIEWS];
+    __shared__ float4 s_hh[HH_F4 * MAX_VIEWS];
     stage_ref(A.refs[r], D, s_hh);
     __syncthreads();
     const int line = gline - A.line_start[r];
@@ -146,6 +153,7 @@ __global__ void __maxnreg__(SweepRegs<HW>::value) sweep_kernel(const __grid_cons
     __shared__ float s_res_f[MAX_VIEWS];  // NCC(view, previous step's depth)
     __shared__ float s_res_r[MAX_VIEWS];  // NCC(view, random depth)
     __shared__ float s_new[MAX_VIEWS];    // refreshed costs
+    __shared__ float2 s_wsl[2];           // slanted planes: the current slopes of steps k, k+1
 
 #define PM_PIXEL(k, x, y)                                    \
     do {                                                     \
@@ -160,6 +168,7 @@ __global__ void __maxnreg__(SweepRegs<HW>::value) sweep_kernel(const __grid_cons
         if (warp == w_load && k + 1 < nsteps) {
             PM_PIXEL(k + 1, xn, yn);
             load_window<W>(D, xn, yn, axis, lane, s_tab[(k + 1) & 1], s_col[(k + 1) & 1], s_win[(k + 1) & 1]);
+            if (PL && lane == 0) s_wsl[(k + 1) & 1] = D.slopes[yn * Wd + xn];
         }
         if (warp == w_draw && k + 2 < nsteps) {
             PM_PIXEL(k + 2, xn, yn);
@@ -169,6 +178,10 @@ __global__ void __maxnreg__(SweepRegs<HW>::value) sweep_kernel(const __grid_cons
 
     float alpha = 0.5f, d_former = 0.0f;
     float c_next = 0.0f, b_next = 0.0f, d_next = 0.0f;
+    // slanted-plane mode: the previous step's slopes and their plane scale at its own pixel
+    // (x, y, s), kept in shared memory by warp 0's lane 0 so that no register holds them across
+    // the NCC passes; a step's current slopes, loaded with its window (s_wsl[k & 1])
+    __shared__ float4 s_former;
     unsigned long long n_alg = 0, n_done = 0;
     if (warp == 0) {
         // backward messages in reverse processing order (patchMatch.cu:856-869, :1050-1059)
@@ -195,6 +208,10 @@ __global__ void __maxnreg__(SweepRegs<HW>::value) sweep_kernel(const __grid_cons
             alpha = msg_forward(0.5f, emission(c, a2), u_emit);
         }
         d_former = D.depth[pix];
+        if (PL && lane == 0) {
+            const float2 sl = D.slopes[pix];
+            s_former = make_float4(sl.x, sl.y, plane_terms(D, sl, (float)x + 0.5f, (float)y + 0.5f).s, 0.0f);
+        }
         if (nsteps > 1) {
             PM_PIXEL(1, x, y);
             const uint32_t p1 = (uint32_t)(y * Wd + x);
@@ -210,6 +227,7 @@ __global__ void __maxnreg__(SweepRegs<HW>::value) sweep_kernel(const __grid_cons
         int x, y;
         PM_PIXEL(1, x, y);
         load_window<W>(D, x, y, axis, lane, s_tab[1], s_col[1], s_win[1]);
+        if (PL && lane == 0) s_wsl[1] = D.slopes[y * Wd + x];
     }
     if (warp == w_draw) {
         for (int k = 1; k < nsteps && k <= 2; ++k) {
@@ -265,10 +283,40 @@ __global__ void __maxnreg__(SweepRegs<HW>::value) sweep_kernel(const __grid_cons
             // search (no counterpart in the reference) half of the pixels instead draw within
             // +-perturb (relative) of their current depth
             float d_rand = fmaf(dr.depth, D.depth_span, D.depth_near);
-            if (A.perturb > 0.0f && dr.mode >= 0.5f)
+            float d_prop = d_former;
+            if (PL) {
+                // slanted planes (lane 0 publishes them): the previous step's plane carried to
+                // this pixel (d s_prev / s_here), and a random hypothesis of one of three kinds
+                if (lane == 0) {
+                    const float lo = D.depth_near, hi = __fadd_rn(D.depth_near, D.depth_span);
+                    const float4 f = s_former;
+                    const float2 sl_f = make_float2(f.x, f.y), sl_cur = s_wsl[buf];
+                    const PlaneG gp = plane_terms(D, sl_f, (float)x + 0.5f, (float)y + 0.5f);
+                    d_prop = fminf(fmaxf(__fmul_rn(d_former, __fmul_rn(f.z, rcp_nr(gp.s))), lo), hi);
+                    float2 sl_r = sl_cur;
+                    if (dr.mode < PLANE_P_DEPTH) {
+                        // a uniform depth with the current slopes (the reference's random depth)
+                    } else if (dr.mode < PLANE_P_SLOPE) {
+                        d_rand = d_cur;
+                        sl_r = make_float2(__fmul_rn(SLOPE_DRAW, fmaf(2.0f, dr.sa, -1.0f)),
+                                           __fmul_rn(SLOPE_DRAW, fmaf(2.0f, dr.sb, -1.0f)));
+                    } else {
+                        const float dstep = __fmul_rn(D.plane_dstep, A.decay);
+                        const float sstep = __fmul_rn(D.plane_sstep, A.decay);
+                        d_rand = fminf(fmaxf(__fmul_rn(d_cur, fmaf(dstep, fmaf(2.0f, dr.depth, -1.0f), 1.0f)), lo), hi);
+                        sl_r.x = fminf(fmaxf(fmaf(sstep, fmaf(2.0f, dr.sa, -1.0f), sl_cur.x), -SLOPE_MAX), SLOPE_MAX);
+                        sl_r.y = fminf(fmaxf(fmaf(sstep, fmaf(2.0f, dr.sb, -1.0f), sl_cur.y), -SLOPE_MAX), SLOPE_MAX);
+                    }
+                    StepCtl &Cp = s_ctl[buf];
+                    Cp.sl_f = sl_f;
+                    Cp.sl_c = sl_cur;
+                    Cp.sl_r = sl_r;
+                }
+            } else if (A.perturb > 0.0f && dr.mode >= 0.5f) {
                 d_rand = fminf(fmaxf(__fmul_rn(d_cur, fmaf(A.perturb, fmaf(2.0f, dr.depth, -1.0f), 1.0f)),
                                      D.depth_near),
                                D.depth_near + D.depth_span);
+            }
             const float u_mine = lane < S ? dr.sample[lane] : 2.0f;
             StepCtl &C = s_ctl[buf];
             unsigned umask = 0;
@@ -290,7 +338,7 @@ __global__ void __maxnreg__(SweepRegs<HW>::value) sweep_kernel(const __grid_cons
                 C.umask = umask;
                 C.tested = tested;
                 C.c1sum = c1;
-                C.d_former = d_former;
+                C.d_former = d_prop;
                 C.d_rand = d_rand;
                 C.d_cur = d_cur;
             }
@@ -315,17 +363,21 @@ __global__ void __maxnreg__(SweepRegs<HW>::value) sweep_kernel(const __grid_cons
             for (int t = task0; t < ntask; t += n_eval) {
                 int va, vb;
                 float da, db;
+                float2 sa, sb;
                 if (phase == 0) {
                     va = vb = nth_bit(umask, t);
                     da = C.d_former;
                     db = C.d_rand;
+                    sa = PL ? C.sl_f : make_float2(0.0f, 0.0f);
+                    sb = PL ? C.sl_r : make_float2(0.0f, 0.0f);
                 } else {
                     va = nth_bit(need, 2 * t);
                     vb = 2 * t + 1 < nn ? nth_bit(need, 2 * t + 1) : va;
                     da = db = best;
+                    sa = sb = PL ? (idx == 0 ? C.sl_f : (idx == 1 ? C.sl_c : C.sl_r)) : make_float2(0.0f, 0.0f);
                 }
                 float ra, rb;
-                ncc_pair<W, HW>(D, s_hh, wc, tab, col, lane, va, da, vb, db, ra, rb);
+                ncc_pair<W, HW, PL>(D, s_hh, wc, tab, col, lane, va, da, sa, vb, db, sb, ra, rb);
                 if (lane == 0) {
                     if (phase == 0) {
                         s_res_f[va] = ra;
@@ -384,6 +436,11 @@ __global__ void __maxnreg__(SweepRegs<HW>::value) sweep_kernel(const __grid_cons
             }
             if (lane == 0) {
                 D.depth[pix] = best;
+                if (PL) {
+                    const float2 sl = idx == 0 ? C.sl_f : (idx == 1 ? C.sl_c : C.sl_r);
+                    D.slopes[pix] = sl;
+                    s_former = make_float4(sl.x, sl.y, plane_terms(D, sl, (float)x + 0.5f, (float)y + 0.5f).s, 0.0f);
+                }
                 n_alg += 2 * tested;
                 n_done += 2 * nu;
             }
@@ -407,12 +464,12 @@ __global__ void __maxnreg__(SweepRegs<HW>::value) sweep_kernel(const __grid_cons
 
 // All views' costs at the current depth for every pixel of one reference; one warp per pixel,
 // two views per pass.
-template <int W, bool HW>
+template <int W, bool HW, bool PL>
 __global__ void __launch_bounds__(COST_BLOCK) costs_kernel(const RefDesc *refs, int r, int axis)
 {
     constexpr int TAB = Window<W>::TAB;
     __shared__ RefDesc D;
-    __shared__ float4 s_hh[5 * MAX_VIEWS];
+    __shared__ float4 s_hh[HH_F4 * MAX_VIEWS];
     stage_ref(refs[r], D, s_hh);
     __syncthreads();
     const int lane = threadIdx.x & 31;
@@ -431,11 +488,12 @@ __global__ void __launch_bounds__(COST_BLOCK) costs_kernel(const RefDesc *refs, 
         load_window<W>(D, x, y, axis, lane, tab, col, wc);
         __syncwarp();
         const float d = D.depth[p];
+        const float2 sl = PL ? D.slopes[p] : make_float2(0.0f, 0.0f);
         float mine = 0.0f;
         for (int v = 0; v < V; v += 2) {
             const int vb = v + 1 < V ? v + 1 : v;
             float na, nb;
-            ncc_pair<W, HW>(D, s_hh, wc, tab, col, lane, v, d, vb, d, na, nb);
+            ncc_pair<W, HW, PL>(D, s_hh, wc, tab, col, lane, v, d, sl, vb, d, sl, na, nb);
             if (lane == v) mine = na;
             if (lane == vb) mine = nb;
         }
@@ -447,15 +505,16 @@ __global__ void __launch_bounds__(COST_BLOCK) costs_kernel(const RefDesc *refs, 
     }
 }
 
-// Windowed NCC for a list of queries, one warp per query.
-template <int W, bool HW>
+// Windowed NCC for a list of queries, one warp per query; slopes (slanted-plane mode) may be
+// null.
+template <int W, bool HW, bool PL>
 __global__ void __launch_bounds__(COST_BLOCK) eval_kernel(const RefDesc *refs, int r, int n,
                                                           const int4 *q, const float *depths,
-                                                          float *out)
+                                                          const float2 *slopes, float *out)
 {
     constexpr int TAB = Window<W>::TAB;
     __shared__ RefDesc D;
-    __shared__ float4 s_hh[5 * MAX_VIEWS];
+    __shared__ float4 s_hh[HH_F4 * MAX_VIEWS];
     stage_ref(refs[r], D, s_hh);
     __syncthreads();
     const int lane = threadIdx.x & 31;
@@ -472,7 +531,8 @@ __global__ void __launch_bounds__(COST_BLOCK) eval_kernel(const RefDesc *refs, i
         load_window<W>(D, t.x, t.y, t.w, lane, tab, col, wc);
         __syncwarp();
         float v, unused;
-        ncc_pair<W, HW>(D, s_hh, wc, tab, col, lane, t.z, depths[i], t.z, depths[i], v, unused);
+        const float2 sl = PL && slopes ? slopes[i] : make_float2(0.0f, 0.0f);
+        ncc_pair<W, HW, PL>(D, s_hh, wc, tab, col, lane, t.z, depths[i], sl, t.z, depths[i], sl, v, unused);
         if (lane == 0) out[i] = v;
     }
 }
@@ -489,13 +549,13 @@ __global__ void __launch_bounds__(COST_BLOCK) eval_kernel(const RefDesc *refs, i
 // One warp per pixel.
 constexpr float REFINE_SQRT3 = 1.7320508075688772f;
 
-template <int W, bool HW>
+template <int W, bool HW, bool PL>
 __global__ void __launch_bounds__(COST_BLOCK) refine_kernel(const RefDesc *refs, int r, int axis, int trials,
                                                             float sigma, uint32_t sweep_id, int samples)
 {
     constexpr int TAB = Window<W>::TAB;
     __shared__ RefDesc D;
-    __shared__ float4 s_hh[5 * MAX_VIEWS];
+    __shared__ float4 s_hh[HH_F4 * MAX_VIEWS];
     stage_ref(refs[r], D, s_hh);
     __syncthreads();
     const int lane = threadIdx.x & 31;
@@ -520,13 +580,14 @@ __global__ void __launch_bounds__(COST_BLOCK) refine_kernel(const RefDesc *refs,
         load_window<W>(D, x, y, axis, lane, tab, col, wc);
         __syncwarp();
         const float d0 = D.depth[p];
+        const float2 sl = PL ? D.slopes[p] : make_float2(0.0f, 0.0f);
         auto score = [&](float dd) {
             float sum = 0.0f;
             for (int t = 0; t < nv; t += 2) {
                 const int va = __shfl_sync(FULL_MASK, my_view, nth_bit(mask, t));
                 const int vb = t + 1 < nv ? __shfl_sync(FULL_MASK, my_view, nth_bit(mask, t + 1)) : va;
                 float na, nb;
-                ncc_pair<W, HW>(D, s_hh, wc, tab, col, lane, va, dd, vb, dd, na, nb);
+                ncc_pair<W, HW, PL>(D, s_hh, wc, tab, col, lane, va, dd, sl, vb, dd, sl, na, nb);
                 sum = __fadd_rn(sum, na);
                 if (t + 1 < nv) sum = __fadd_rn(sum, nb);
             }

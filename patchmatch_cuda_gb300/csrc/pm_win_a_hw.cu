@@ -2,4 +2,5 @@
 #define PM_GROUP_FN launch_group_a_hw
 #define PM_HW true
 #define PM_WINDOW_LIST(X) X(3) X(5) X(7) X(9) X(11)
+#define PM_PL false
 #include "pm_windows.inc"

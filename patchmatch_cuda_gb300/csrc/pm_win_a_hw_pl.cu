@@ -1,0 +1,6 @@
+// Window sides 3..11 of the window-templated kernels, texture-filtering sampler, slanted planes per pixel.
+#define PM_GROUP_FN launch_group_a_hw_pl
+#define PM_HW true
+#define PM_WINDOW_LIST(X) X(3) X(5) X(7) X(9) X(11)
+#define PM_PL true
+#include "pm_windows.inc"

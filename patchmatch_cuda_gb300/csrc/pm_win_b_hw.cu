@@ -2,4 +2,5 @@
 #define PM_GROUP_FN launch_group_b_hw
 #define PM_HW true
 #define PM_WINDOW_LIST(X) X(13) X(15) X(17)
+#define PM_PL false
 #include "pm_windows.inc"

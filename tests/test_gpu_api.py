@@ -93,7 +93,8 @@ def test_transpose_layers(engine_lib):
     assert torch.equal(y, want)
 
 
-def test_cli_matches_the_library(small, tmp_path):
+@pytest.mark.parametrize("planes", [0, 1])
+def test_cli_matches_the_library(small, tmp_path, planes):
     from patchmatch_cuda_gb300 import _native, load_depth_file, write_middlebury, write_pgm
     names = []
     for i, im in enumerate(small.images):
@@ -107,11 +108,12 @@ def test_cli_matches_the_library(small, tmp_path):
         f"refImageId = {small.ref_id}\nhalfWindowSize = {w.half_window}\nnumOfSamples = {w.num_samples}\n"
         f"SPMAlpha = {w.sp_alpha}\ngaussianSigma = {w.gaussian_sigma}\nnumOfIterations = {w.iterations}\n"
         f"depthRangeNear = {w.depth_near}\ndepthRangeFar = {w.depth_far}\n"
-        f"outputFileName = {tmp_path / 'depth.bin'}\nprefilter = {w.prefilter}\nseed = {w.seed}\n")
+        f"outputFileName = {tmp_path / 'depth.bin'}\nprefilter = {w.prefilter}\nseed = {w.seed}\n"
+        f"planes = {planes}\n")
     r = subprocess.run([str(_native.LIB_DIR / "pm_cli"), str(tmp_path / "run.ini")], capture_output=True,
                        text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
-    eng = _engine(small)
+    eng = _engine(small, planes=planes)
     eng.run()
     np.testing.assert_array_equal(load_depth_file(tmp_path / "depth.bin"), eng.depth())
     eng.close()
