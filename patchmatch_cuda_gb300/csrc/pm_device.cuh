@@ -433,9 +433,9 @@ __device__ __forceinline__ void column_moments(const WarpSetup &A, cudaTextureOb
             j = fetch<HW>(tex, layer, sw, sh, fmaf(A.c1x, fdy, colx), fmaf(A.c1y, fdy, coly),
                           fmaf(A.c1z, fdy, colz));
         const float b = tab[dy * W + cc];
-        // the shift: the sample of the first row inside the reference image (row 0 of a full
-        // window), so that K = 0 and s2 = 0 say exactly that every in-bounds sample is zero
-        if (FULL ? dy == 0 : dy == wc.dy_lo) m.k = j;
+        // the shift: row 0's sample, or 0 when row 0 lies outside the reference image (a window
+        // cut at the top), so that K = 0 and s2 = 0 say exactly that every in-bounds sample is 0
+        if (dy == 0) m.k = (FULL || wc.dy_lo == 0) ? j : 0.0f;
         // lanes off the window's columns fetch nothing: j = K = 0 there
         const float d = (FULL || (dy >= wc.dy_lo && dy <= wc.dy_hi)) ? j - m.k : 0.0f;
         m.s1 += d;

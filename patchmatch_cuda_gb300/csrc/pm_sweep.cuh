@@ -59,8 +59,13 @@ struct StepCtl {
     int tested;              // samples that found a view
     float c1sum;             // sum of the drawn views' current costs, in draw order
     float d_former, d_rand, d_cur;
-    float2 sl_f, sl_c, sl_r;  // slanted-plane mode: slopes of the three hypotheses
     int8_t sel[MAX_VIEWS];   // view of each draw, -1 when the CDF found none
+};
+
+// Slanted-plane mode: slopes of a step's three hypotheses (former, current, random), beside its
+// StepCtl (only the plane-mode kernels use it).
+struct PlaneCtl {
+    float2 sl_f, sl_c, sl_r;
 };
 
 // The view-sample and random-depth draws of one step, made one step ahead (double-buffered).
@@ -69,34 +74,45 @@ struct StepDraws {
     float sample[MAX_VIEWS];  // view samples (RNG_SAMPLE)
     float depth;              // random depth (RNG_RAND_DEPTH, first word)
     float mode;               // local or global random search (RNG_RAND_DEPTH, second word)
-    float sa, sb;             // slanted planes: random slopes (RNG_RAND_DEPTH, words 3 and 4)
 };
 
+// One Philox counter per drawing lane (a single call site, so the lanes do not diverge). PL: the
+// random-depth counter's third and fourth words go to *slopes (random slopes).
+template <bool PL>
 __device__ __forceinline__ void make_draws(const RefDesc &D, uint32_t pix, uint32_t sweep, int S,
-                                           int lane, StepDraws &out)
+                                           int lane, StepDraws &out, float2 *slopes)
 {
     const uint64_t seed = D.seed;
     const uint32_t batch = D.batch_id;
     // lanes below S draw the view samples; the last lane the random depth (when S < 32)
     const bool depth_lane = lane == 31 && S < 32;
     if (lane < S || depth_lane) {
-        const float4 u = draw_uniform4(seed, pix, sweep, depth_lane ? RNG_RAND_DEPTH : RNG_SAMPLE,
-                                       depth_lane ? 0 : lane, batch);
-        if (depth_lane) {
-            out.depth = u.x;
-            out.mode = u.y;
-            out.sa = u.z;
-            out.sb = u.w;
+        if (PL) {
+            const float4 u = draw_uniform4(seed, pix, sweep, depth_lane ? RNG_RAND_DEPTH : RNG_SAMPLE,
+                                           depth_lane ? 0 : lane, batch);
+            if (depth_lane) {
+                out.depth = u.x;
+                out.mode = u.y;
+                *slopes = make_float2(u.z, u.w);
+            } else {
+                out.sample[lane] = u.x;
+            }
         } else {
-            out.sample[lane] = u.x;
+            const float2 u = draw_uniform2(seed, pix, sweep, depth_lane ? RNG_RAND_DEPTH : RNG_SAMPLE,
+                                           depth_lane ? 0 : lane, batch);
+            if (depth_lane) {
+                out.depth = u.x;
+                out.mode = u.y;
+            } else {
+                out.sample[lane] = u.x;
+            }
         }
     }
     if (S >= 32 && lane == 0) {
         const float4 u = draw_uniform4(seed, pix, sweep, RNG_RAND_DEPTH, 0, batch);
         out.depth = u.x;
         out.mode = u.y;
-        out.sa = u.z;
-        out.sb = u.w;
+        if (PL) *slopes = make_float2(u.z, u.w);
     }
 }
 
@@ -154,6 +170,8 @@ __global__ void __maxnreg__(SweepRegs<HW>::value) sweep_kernel(const __grid_cons
     __shared__ float s_res_r[MAX_VIEWS];  // NCC(view, random depth)
     __shared__ float s_new[MAX_VIEWS];    // refreshed costs
     __shared__ float2 s_wsl[2];           // slanted planes: the current slopes of steps k, k+1
+    __shared__ float2 s_dsl[3];           // slanted planes: random-slope draws of steps k .. k+2
+    __shared__ PlaneCtl s_pctl[2];        // slanted planes: the hypotheses' slopes
 
 #define PM_PIXEL(k, x, y)                                    \
     do {                                                     \
@@ -172,7 +190,7 @@ __global__ void __maxnreg__(SweepRegs<HW>::value) sweep_kernel(const __grid_cons
         }
         if (warp == w_draw && k + 2 < nsteps) {
             PM_PIXEL(k + 2, xn, yn);
-            make_draws(D, (uint32_t)(yn * Wd + xn), sweep, S, lane, s_draw[(k + 2) % 3]);
+            make_draws<PL>(D, (uint32_t)(yn * Wd + xn), sweep, S, lane, s_draw[(k + 2) % 3], &s_dsl[(k + 2) % 3]);
         }
     };
 
@@ -233,7 +251,7 @@ __global__ void __maxnreg__(SweepRegs<HW>::value) sweep_kernel(const __grid_cons
         for (int k = 1; k < nsteps && k <= 2; ++k) {
             int x, y;
             PM_PIXEL(k, x, y);
-            make_draws(D, (uint32_t)(y * Wd + x), sweep, S, lane, s_draw[k]);
+            make_draws<PL>(D, (uint32_t)(y * Wd + x), sweep, S, lane, s_draw[k], &s_dsl[k]);
         }
     }
     __syncthreads();
@@ -293,24 +311,25 @@ __global__ void __maxnreg__(SweepRegs<HW>::value) sweep_kernel(const __grid_cons
                     const float2 sl_f = make_float2(f.x, f.y), sl_cur = s_wsl[buf];
                     const PlaneG gp = plane_terms(D, sl_f, (float)x + 0.5f, (float)y + 0.5f);
                     d_prop = fminf(fmaxf(__fmul_rn(d_former, __fmul_rn(f.z, rcp_nr(gp.s))), lo), hi);
+                    const float2 u = s_dsl[k % 3];
                     float2 sl_r = sl_cur;
                     if (dr.mode < PLANE_P_DEPTH) {
                         // a uniform depth with the current slopes (the reference's random depth)
                     } else if (dr.mode < PLANE_P_SLOPE) {
                         d_rand = d_cur;
-                        sl_r = make_float2(__fmul_rn(SLOPE_DRAW, fmaf(2.0f, dr.sa, -1.0f)),
-                                           __fmul_rn(SLOPE_DRAW, fmaf(2.0f, dr.sb, -1.0f)));
+                        sl_r = make_float2(__fmul_rn(SLOPE_DRAW, fmaf(2.0f, u.x, -1.0f)),
+                                           __fmul_rn(SLOPE_DRAW, fmaf(2.0f, u.y, -1.0f)));
                     } else {
                         const float dstep = __fmul_rn(D.plane_dstep, A.decay);
                         const float sstep = __fmul_rn(D.plane_sstep, A.decay);
                         d_rand = fminf(fmaxf(__fmul_rn(d_cur, fmaf(dstep, fmaf(2.0f, dr.depth, -1.0f), 1.0f)), lo), hi);
-                        sl_r.x = fminf(fmaxf(fmaf(sstep, fmaf(2.0f, dr.sa, -1.0f), sl_cur.x), -SLOPE_MAX), SLOPE_MAX);
-                        sl_r.y = fminf(fmaxf(fmaf(sstep, fmaf(2.0f, dr.sb, -1.0f), sl_cur.y), -SLOPE_MAX), SLOPE_MAX);
+                        sl_r.x = fminf(fmaxf(fmaf(sstep, fmaf(2.0f, u.x, -1.0f), sl_cur.x), -SLOPE_MAX), SLOPE_MAX);
+                        sl_r.y = fminf(fmaxf(fmaf(sstep, fmaf(2.0f, u.y, -1.0f), sl_cur.y), -SLOPE_MAX), SLOPE_MAX);
                     }
-                    StepCtl &Cp = s_ctl[buf];
-                    Cp.sl_f = sl_f;
-                    Cp.sl_c = sl_cur;
-                    Cp.sl_r = sl_r;
+                    PlaneCtl &P = s_pctl[buf];
+                    P.sl_f = sl_f;
+                    P.sl_c = sl_cur;
+                    P.sl_r = sl_r;
                 }
             } else if (A.perturb > 0.0f && dr.mode >= 0.5f) {
                 d_rand = fminf(fmaxf(__fmul_rn(d_cur, fmaf(A.perturb, fmaf(2.0f, dr.depth, -1.0f), 1.0f)),
@@ -368,13 +387,13 @@ __global__ void __maxnreg__(SweepRegs<HW>::value) sweep_kernel(const __grid_cons
                     va = vb = nth_bit(umask, t);
                     da = C.d_former;
                     db = C.d_rand;
-                    sa = PL ? C.sl_f : make_float2(0.0f, 0.0f);
-                    sb = PL ? C.sl_r : make_float2(0.0f, 0.0f);
+                    sa = PL ? s_pctl[buf].sl_f : make_float2(0.0f, 0.0f);
+                    sb = PL ? s_pctl[buf].sl_r : make_float2(0.0f, 0.0f);
                 } else {
                     va = nth_bit(need, 2 * t);
                     vb = 2 * t + 1 < nn ? nth_bit(need, 2 * t + 1) : va;
                     da = db = best;
-                    sa = sb = PL ? (idx == 0 ? C.sl_f : (idx == 1 ? C.sl_c : C.sl_r)) : make_float2(0.0f, 0.0f);
+                    sa = sb = PL ? (idx == 0 ? s_pctl[buf].sl_f : s_pctl[buf].sl_r) : make_float2(0.0f, 0.0f);
                 }
                 float ra, rb;
                 ncc_pair<W, HW, PL>(D, s_hh, wc, tab, col, lane, va, da, sa, vb, db, sb, ra, rb);
@@ -437,7 +456,8 @@ __global__ void __maxnreg__(SweepRegs<HW>::value) sweep_kernel(const __grid_cons
             if (lane == 0) {
                 D.depth[pix] = best;
                 if (PL) {
-                    const float2 sl = idx == 0 ? C.sl_f : (idx == 1 ? C.sl_c : C.sl_r);
+                    const PlaneCtl &P = s_pctl[buf];
+                    const float2 sl = idx == 0 ? P.sl_f : (idx == 1 ? P.sl_c : P.sl_r);
                     D.slopes[pix] = sl;
                     s_former = make_float4(sl.x, sl.y, plane_terms(D, sl, (float)x + 0.5f, (float)y + 0.5f).s, 0.0f);
                 }
