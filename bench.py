@@ -49,6 +49,7 @@ def parse_args():
     ap.add_argument("--profile", type=int, default=None, metavar="DIR",
                     help="run only the initial state and one sweep in direction DIR (for ncu)")
     ap.add_argument("--threads-per-line", type=int, default=0)
+    ap.add_argument("--planes", type=int, default=0, help="--profile: slanted planes per pixel (1)")
     ap.add_argument("--learned", type=int, default=0, metavar="SWEEPS",
                     help="batched workloads: learned initialisation followed by SWEEPS sweeps")
     ap.add_argument("--profile-net", action="store_true",
@@ -62,7 +63,7 @@ def run_profile(args):
     wl = scene.WORKLOADS[args.workload]
     sv = scene.make_views(wl)
     eng = Engine(sv.images, sv.ref_id, wl.params(precision=args.precision,
-                                                  threads_per_line=args.threads_per_line))
+                                                  threads_per_line=args.threads_per_line, planes=args.planes))
     eng.init_depth()
     eng.compute_costs(1)
     eng.run_sweep(args.profile, 4 + args.profile, wl.num_samples)
@@ -485,6 +486,12 @@ def learned_vs_plain(sv, wl, device, flush, reps):
     runs = [("plain_20_sweeps", dict()),
             ("learned_4_sweeps", dict(init_mode=INIT_PROPOSAL, num_sweeps=4, perturbation=0.05)),
             ("learned_8_sweeps", dict(init_mode=INIT_PROPOSAL, num_sweeps=8, perturbation=0.05)),
+            # control: the learned schedule with every pixel from the random initialisation
+            # (confidence threshold 1), i.e. what the network itself contributes
+            ("control_random_init_4_sweeps", dict(init_mode=INIT_PROPOSAL, proposal_threshold=1.0, num_sweeps=4,
+                                                  perturbation=0.05)),
+            ("control_random_init_8_sweeps", dict(init_mode=INIT_PROPOSAL, proposal_threshold=1.0, num_sweeps=8,
+                                                  perturbation=0.05)),
             # the refinement step after the last sweep (the reference's never-launched kernel's
             # 10 trials of sigma 0.05, and a finer 16 x 0.02)
             ("plain_20_sweeps_refine_10x0.05", dict(refine_trials=10, refine_sigma=0.05)),
@@ -494,6 +501,7 @@ def learned_vs_plain(sv, wl, device, flush, reps):
                                                      refine_trials=16, refine_sigma=0.02))]
     params = proposal.load_params()
     net_ms = gflop = None
+    net_quality = None
     for name, over in runs:
         e = Engine(sv.images, sv.ref_id, wl.params(gpu_id=device, **over))
         learned = over.get("init_mode") == INIT_PROPOSAL
@@ -522,6 +530,20 @@ def learned_vs_plain(sv, wl, device, flush, reps):
                 t.append(e0.elapsed_time(e1))
             net_ms = statistics.median(t)
             gflop = proposal.forward_flops(hp, wp) / 1e9
+            # the network's own prediction: confident fraction and its depth error there (4x4
+            # blocks, harmonic mean of the ground truth)
+            o = y.cpu().numpy().astype(np.float64)
+            h4, w4 = e.height // 4, e.width // 4
+            conf, s_ = o[:h4, :w4, 1], o[:h4, :w4, 0]
+            thr = e.params.proposal_threshold
+            inv_far, inv_range = 1.0 / wl.depth_far, 1.0 / wl.depth_near - 1.0 / wl.depth_far
+            dn = 1.0 / (inv_far + s_ * inv_range)
+            g4 = 1.0 / (1.0 / sv.gt_depth[:4 * h4, :4 * w4].reshape(h4, 4, w4, 4)).mean(axis=(1, 3))
+            rel = np.abs(dn - g4) / g4
+            net_quality = {"confident_fraction": round(float(np.mean(conf >= thr)), 4),
+                           "median_rel_err_pct_confident": round(100 * float(np.median(rel[conf >= thr])), 2)
+                           if np.any(conf >= thr) else None,
+                           "median_rel_err_pct_all": round(100 * float(np.median(rel)), 2)}
         e.close()
         if net is not None:
             net.close()
@@ -533,6 +555,7 @@ def learned_vs_plain(sv, wl, device, flush, reps):
     out["network_forward"] = {"ms": round(net_ms, 4), "gflop": round(gflop, 3), "tflops": round(tflops, 3),
                               "peak_tflops": peak, "frac_of_bf16_peak": round(tflops / peak, 5),
                               "peak_source": "MEASURED_PEAKS.json bf16_tflops (cuBLAS burst)"}
+    out["network_prediction"] = net_quality
     return out
 
 
