@@ -246,6 +246,28 @@ struct WinCtl {
     int dy_lo, dy_hi;    // in-bounds rows
 };
 
+// The scalar part of a window (lane 0 of the loading warp): origin, plane scale, c1, 1 / n,
+// the in-bounds rows [cy0, cy1], the leading-edge term bsum, and whether it lies inside the image.
+__device__ __forceinline__ void window_scalars(const RefDesc &D, int x, int y, int x0, int y0, int cy0, int cy1,
+                                               float n, size_t pix, float bsum, bool full, WinCtl &wc)
+{
+    wc.ox = (float)x0 + 0.5f;
+    wc.oy = (float)y0 + 0.5f;
+    // explicit IEEE operations: the texture-filtering sampler's coordinates are replicated bit
+    // for bit by the oracle
+    wc.scale = __fadd_rn(__fmul_rn(D.nx, fmaf(D.ik00, __fadd_rn((float)x, 0.5f), D.ik02)), D.nz);
+    wc.c1 = __ldg(D.c1 + pix);
+    wc.inv_n = 1.0f / n;
+    wc.rows = (float)(cy1 - cy0 + 1);
+    wc.inv_rows = 1.0f / wc.rows;
+    wc.bsum = bsum;
+    wc.x0 = x0;
+    wc.y0 = y0;
+    wc.full = full;
+    wc.dy_lo = cy0 - y0;
+    wc.dy_hi = cy1 - y0;
+}
+
 // Loads pixel (x, y)'s window with one warp, lane c owning columns c and c + 32. axis selects
 // which image axis is the sweep's column axis for the leading-edge shift (0: x, vertical
 // sweeps; 1: y).
@@ -300,24 +322,65 @@ __device__ __forceinline__ void load_window(const RefDesc &D, int x, int y, int 
         col[c] = cs;
     }
     if (shifted) sh = warp_sum(sh);
-    if (lane == 0) {
-        wc.ox = (float)x0 + 0.5f;
-        wc.oy = (float)y0 + 0.5f;
+    if (lane == 0)
+        window_scalars(D, x, y, x0, y0, cy0, cy1, n, pix, shifted ? sh : 0.0f,
+                       x0 >= 0 && y0 >= 0 && x + HW < Wd && y + HW < Hd, wc);
+}
 
-        // explicit IEEE operations: the texture-filtering sampler's coordinates are
-        // replicated bit for bit by the oracle
-        wc.scale = __fadd_rn(__fmul_rn(D.nx, fmaf(D.ik00, __fadd_rn((float)x, 0.5f), D.ik02)), D.nz);
-        wc.c1 = __ldg(D.c1 + pix);
-        wc.inv_n = 1.0f / n;
-        wc.rows = (float)(cy1 - cy0 + 1);
-        wc.inv_rows = 1.0f / wc.rows;
-        wc.bsum = shifted ? sh : 0.0f;
-        wc.x0 = x0;
-        wc.y0 = y0;
-        wc.full = x0 >= 0 && y0 >= 0 && x + HW < Wd && y + HW < Hd;
-        wc.dy_lo = cy0 - y0;
-        wc.dy_hi = cy1 - y0;
+// The sweep kernel's sliding form of load_window for windows inside the image. The raw
+// reference values of the current window live in a ring `raw` of W x W floats indexed by image
+// line modulo W (filled by load_window), so a step of a sweep loads only the line that enters
+// the window:
+//   rows (vertical sweeps):     raw[(yy % W) * W + c]  = R(x0 + c, yy)
+//   columns (horizontal ones):  raw[dy * W + (xx % W)] = R(xx, y0 + dy)
+// `enter` is the image row (rows) or column that entered since the previous step, or -1 to fill
+// the whole ring (a step whose previous window was cut by the border). The table and
+// column sums are then formed from the ring with load_window's arithmetic in its order, so both
+// give the same values.
+template <int W>
+__device__ __forceinline__ void ring_window(const RefDesc &D, int x, int y, bool rows, int enter, int lane,
+                                            float *raw, float *tab, float *col, WinCtl &wc)
+{
+    constexpr int HW = Window<W>::HW;
+    const int Wd = D.width;
+    const int x0 = x - HW, y0 = y - HW;
+#pragma unroll
+    for (int q = 0; q < (W + 31) / 32; ++q) {
+        const int c = lane + 32 * q;  // a window column, or a window row for an entering column
+        if (c >= W) continue;
+        if (enter < 0) {
+            // one value at a time (a fill happens once per run of inside windows)
+#pragma unroll 1
+            for (int dy = 0; dy < W; ++dy) {
+                const float r = __ldg(D.ref + (size_t)(y0 + dy) * Wd + x0 + c);
+                raw[rows ? ((y0 + dy) % W) * W + c : dy * W + (x0 + c) % W] = r;
+            }
+        } else if (rows) {
+            raw[(enter % W) * W + c] = __ldg(D.ref + (size_t)enter * Wd + x0 + c);
+        } else {
+            raw[c * W + enter % W] = __ldg(D.ref + (size_t)(y0 + c) * Wd + enter);
+        }
     }
+    __syncwarp();
+    const float n = (float)(W * W);
+    const size_t pix = (size_t)y * Wd + x;
+    const float mu = __ldg(D.sum_i + pix) / n;
+#pragma unroll
+    for (int q = 0; q < (W + 31) / 32; ++q) {
+        const int c = lane + 32 * q;
+        if (c >= W) continue;
+        const int cslot = (x0 + c) % W;
+        int rslot = y0 % W;
+        float cs = 0.0f;
+        for (int dy = 0; dy < W; ++dy) {
+            const float b = (rows ? raw[rslot * W + c] : raw[dy * W + cslot]) - mu;
+            rslot = rslot + 1 == W ? 0 : rslot + 1;
+            tab[dy * W + c] = b;
+            cs += b;
+        }
+        col[c] = cs;
+    }
+    if (lane == 0) window_scalars(D, x, y, x0, y0, y0, y0 + W - 1, n, pix, 0.0f, true, wc);
 }
 
 // A homography's first two columns and its value at the window origin (see warp_setup).

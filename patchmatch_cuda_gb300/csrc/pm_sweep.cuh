@@ -169,6 +169,7 @@ __global__ void __maxnreg__(SweepRegs<HW>::value) sweep_kernel(const __grid_cons
     __shared__ float s_res_f[MAX_VIEWS];  // NCC(view, previous step's depth)
     __shared__ float s_res_r[MAX_VIEWS];  // NCC(view, random depth)
     __shared__ float s_new[MAX_VIEWS];    // refreshed costs
+    __shared__ float s_raw[W * W];        // reference values of the current interior window
     __shared__ float2 s_wsl[2];           // slanted planes: the current slopes of steps k, k+1
     __shared__ float2 s_dsl[3];           // slanted planes: random-slope draws of steps k .. k+2
     __shared__ PlaneCtl s_pctl[2];        // slanted planes: the hypotheses' slopes
@@ -180,13 +181,29 @@ __global__ void __maxnreg__(SweepRegs<HW>::value) sweep_kernel(const __grid_cons
         y = rot ? line : c_;                                 \
     } while (0)
 
+    // step kk's window (loader warp): inside the image from the ring s_raw, sliding it by the
+    // entering line when it holds the previous step's window, otherwise loaded whole
+    constexpr int HWIN = Window<W>::HW;
+    int ring_step = -1;  // the step whose window the ring holds
+    auto load_step = [&](int kk, int xn, int yn) {
+        if (xn >= HWIN && yn >= HWIN && xn + HWIN < Wd && yn + HWIN < Hd) {
+            const int enter = ring_step != kk - 1 ? -1
+                              : rot ? (fwd ? xn + HWIN : xn - HWIN) : (fwd ? yn + HWIN : yn - HWIN);
+            ring_window<W>(D, xn, yn, !rot, enter, lane, s_raw, s_tab[kk & 1], s_col[kk & 1], s_win[kk & 1]);
+            ring_step = kk;
+        } else {
+            load_window<W>(D, xn, yn, axis, lane, s_tab[kk & 1], s_col[kk & 1], s_win[kk & 1]);
+            ring_step = -1;
+        }
+        if (PL && lane == 0) s_wsl[kk & 1] = D.slopes[yn * Wd + xn];
+    };
+
     // step k+1's window and step k+2's draws
     auto prep_step = [&](int k) {
         int xn, yn;
         if (warp == w_load && k + 1 < nsteps) {
             PM_PIXEL(k + 1, xn, yn);
-            load_window<W>(D, xn, yn, axis, lane, s_tab[(k + 1) & 1], s_col[(k + 1) & 1], s_win[(k + 1) & 1]);
-            if (PL && lane == 0) s_wsl[(k + 1) & 1] = D.slopes[yn * Wd + xn];
+            load_step(k + 1, xn, yn);
         }
         if (warp == w_draw && k + 2 < nsteps) {
             PM_PIXEL(k + 2, xn, yn);
@@ -244,8 +261,7 @@ __global__ void __maxnreg__(SweepRegs<HW>::value) sweep_kernel(const __grid_cons
     if (warp == w_load && nsteps > 1) {
         int x, y;
         PM_PIXEL(1, x, y);
-        load_window<W>(D, x, y, axis, lane, s_tab[1], s_col[1], s_win[1]);
-        if (PL && lane == 0) s_wsl[1] = D.slopes[y * Wd + x];
+        load_step(1, x, y);
     }
     if (warp == w_draw) {
         for (int k = 1; k < nsteps && k <= 2; ++k) {
