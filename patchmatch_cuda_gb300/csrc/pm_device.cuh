@@ -249,14 +249,14 @@ struct WinCtl {
 // The scalar part of a window (lane 0 of the loading warp): origin, plane scale, c1, 1 / n,
 // the in-bounds rows [cy0, cy1], the leading-edge term bsum, and whether it lies inside the image.
 __device__ __forceinline__ void window_scalars(const RefDesc &D, int x, int y, int x0, int y0, int cy0, int cy1,
-                                               float n, size_t pix, float bsum, bool full, WinCtl &wc)
+                                               float n, float c1, float bsum, bool full, WinCtl &wc)
 {
     wc.ox = (float)x0 + 0.5f;
     wc.oy = (float)y0 + 0.5f;
     // explicit IEEE operations: the texture-filtering sampler's coordinates are replicated bit
     // for bit by the oracle
     wc.scale = __fadd_rn(__fmul_rn(D.nx, fmaf(D.ik00, __fadd_rn((float)x, 0.5f), D.ik02)), D.nz);
-    wc.c1 = __ldg(D.c1 + pix);
+    wc.c1 = c1;
     wc.inv_n = 1.0f / n;
     wc.rows = (float)(cy1 - cy0 + 1);
     wc.inv_rows = 1.0f / wc.rows;
@@ -323,7 +323,7 @@ __device__ __forceinline__ void load_window(const RefDesc &D, int x, int y, int 
     }
     if (shifted) sh = warp_sum(sh);
     if (lane == 0)
-        window_scalars(D, x, y, x0, y0, cy0, cy1, n, pix, shifted ? sh : 0.0f,
+        window_scalars(D, x, y, x0, y0, cy0, cy1, n, __ldg(D.c1 + pix), shifted ? sh : 0.0f,
                        x0 >= 0 && y0 >= 0 && x + HW < Wd && y + HW < Hd, wc);
 }
 
@@ -344,6 +344,10 @@ __device__ __forceinline__ void ring_window(const RefDesc &D, int x, int y, bool
     constexpr int HW = Window<W>::HW;
     const int Wd = D.width;
     const int x0 = x - HW, y0 = y - HW;
+    // the window's box sum and c1 load together with the entering line: one round trip
+    const size_t pix = (size_t)y * Wd + x;
+    const float sum_i = __ldg(D.sum_i + pix);
+    const float c1 = lane == 0 ? __ldg(D.c1 + pix) : 0.0f;
 #pragma unroll
     for (int q = 0; q < (W + 31) / 32; ++q) {
         const int c = lane + 32 * q;  // a window column, or a window row for an entering column
@@ -363,8 +367,7 @@ __device__ __forceinline__ void ring_window(const RefDesc &D, int x, int y, bool
     }
     __syncwarp();
     const float n = (float)(W * W);
-    const size_t pix = (size_t)y * Wd + x;
-    const float mu = __ldg(D.sum_i + pix) / n;
+    const float mu = sum_i / n;
 #pragma unroll
     for (int q = 0; q < (W + 31) / 32; ++q) {
         const int c = lane + 32 * q;
@@ -380,7 +383,7 @@ __device__ __forceinline__ void ring_window(const RefDesc &D, int x, int y, bool
         }
         col[c] = cs;
     }
-    if (lane == 0) window_scalars(D, x, y, x0, y0, y0, y0 + W - 1, n, pix, 0.0f, true, wc);
+    if (lane == 0) window_scalars(D, x, y, x0, y0, y0, y0 + W - 1, n, c1, 0.0f, true, wc);
 }
 
 // A homography's first two columns and its value at the window origin (see warp_setup).
