@@ -228,3 +228,34 @@ def test_slopes_need_plane_mode(small_scene):
     with pytest.raises(PatchMatchError, match="STATE"):
         eng.eval_costs_planes([1], [1], [0], [3.0], [[0.0, 0.0]], [0])
     eng.close()
+
+
+def test_learned_initialisation_with_planes(small_scene):
+    """A learned initialisation in plane mode: pixels taken from the network start
+    fronto-parallel, the others exactly as the random initialisation (threshold 1: all of
+    them), and a short run keeps depths in range and slopes finite."""
+    from patchmatch_cuda_gb300 import INIT_PROPOSAL, proposal
+    rnd = make_engine(small_scene, sampler=1)
+    orc = oracle_for(rnd, small_scene)
+    want_slopes = orc.init_planes()
+    rnd.init_depth()
+    want_depth = rnd.depth()
+    all_rand = make_engine(small_scene, sampler=1, init_mode=INIT_PROPOSAL, proposal_threshold=1.0)
+    all_net = make_engine(small_scene, sampler=1, init_mode=INIT_PROPOSAL, proposal_threshold=0.0, num_sweeps=2)
+    hp, wp = all_rand.proposal_shape()
+    net = proposal.ProposalNet(1, hp, wp, seed=3)
+    all_rand.set_proposal(net)
+    all_net.set_proposal(net)
+    all_rand.init_depth()
+    np.testing.assert_array_equal(all_rand.slopes(), want_slopes)
+    np.testing.assert_array_equal(all_rand.depth(), want_depth)
+    all_net.init_depth()
+    assert np.all(all_net.slopes() == 0.0)
+    all_net.run()
+    d, s = all_net.depth(), all_net.slopes()
+    w = small_scene.workload
+    assert np.all(np.isfinite(d)) and d.min() >= w.depth_near and d.max() <= w.depth_far
+    assert np.all(np.isfinite(s)) and np.abs(s).max() <= 2.0
+    for e in (rnd, all_rand, all_net):
+        e.close()
+    net.close()
