@@ -121,8 +121,8 @@ bool inv3(const double *m, double *o)
 void relative_homographies(const pm_view &ref, const double *k_ref_inv, const pm_view &src,
                            double nx, double nz, double out[18], double *e_out = nullptr)
 {
-    double kr[9], rr[9], tr[3], ks[9], rs[9], ts[3];
-    for (int i = 0; i < 9; ++i) { rr[i] = ref.R[i]; ks[i] = src.K[i]; rs[i] = src.R[i]; kr[i] = ref.K[i]; }
+    double rr[9], tr[3], ks[9], rs[9], ts[3];
+    for (int i = 0; i < 9; ++i) { rr[i] = ref.R[i]; ks[i] = src.K[i]; rs[i] = src.R[i]; }
     for (int i = 0; i < 3; ++i) { tr[i] = ref.t[i]; ts[i] = src.t[i]; }
     double cr[3], cs[3], rrt[9], rrel[9], h1[9];
     for (int i = 0; i < 3; ++i) {
@@ -144,7 +144,6 @@ void relative_homographies(const pm_view &ref, const double *k_ref_inv, const pm
         for (int j = 0; j < 3; ++j) out[9 + 3 * i + j] = kt[i] * nk[j];
     if (e_out)
         for (int i = 0; i < 3; ++i) e_out[i] = kt[i];
-    (void)kr;
 }
 
 // Prefilter taps (GaussianBlurCUDA.cu:99-130).
