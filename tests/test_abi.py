@@ -69,6 +69,8 @@ def _create(views, ref_id, **over):
     (dict(prefilter=2, gaussian_sigma=0.0), 1), (dict(precision=5), 1),
     (dict(refine_trials=-1), 1), (dict(refine_trials=257), 1), (dict(refine_trials=4, refine_sigma=0.0), 1),
     (dict(refine_trials=4, refine_sigma=float("inf")), 1),
+    (dict(planes=2), 1), (dict(planes=1, plane_depth_step=1.0), 1), (dict(planes=1, plane_depth_step=-0.1), 1),
+    (dict(planes=1, plane_slope_step=2.5), 1), (dict(planes=1, plane_slope_step=float("nan")), 1),
 ])
 def test_invalid_parameters_are_rejected(engine_lib, over, status):
     assert _create(_views(), 0, **over) == status

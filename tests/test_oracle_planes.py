@@ -89,3 +89,48 @@ def test_planes_sharpen_depths_on_slanted_surfaces(oracle_lib, plane_scene):
     assert med_pl < 0.85 * med_ref, (med_pl, med_ref)
     assert scene.bad_pixel_rate(d_pl.astype(np.float32), gt) <= scene.bad_pixel_rate(d_ref.astype(np.float32), gt)
     assert np.all(np.abs(slopes) <= O.SLOPE_MAX)
+
+
+def test_the_true_plane_scores_better_than_fronto_and_mirrored_planes(oracle_lib, plane_scene):
+    """Sign and convention check of the plane geometry on the scene's slanted planes: the plane
+    taken from the ground truth's inverse-depth gradient (1/d = g_u u + g_v v + 1/rho in
+    normalised coordinates, slopes (a, b) = rho (g_u, g_v)) scores a lower median NCC at the true
+    depth than the fronto-parallel plane, and beats the mirrored slopes (-a, -b) on most pixels.
+    With 11x11 windows and a 15 degree arc the differences are small (about 2 % of the cost; the
+    scene's planes tilt by up to 25 degrees), so the test uses many pixels with slopes above
+    0.25."""
+    w = plane_scene.workload
+    gt = plane_scene.gt_depth.astype(np.float64)
+    orc = oracle(plane_scene, planes=1)
+    ik00, ik02, ik11, ik12 = orc.p.inv_k
+    inv = 1.0 / gt
+    gx = np.zeros_like(inv)
+    gy = np.zeros_like(inv)
+    gx[:, 1:-1] = (inv[:, 2:] - inv[:, :-2]) / 2.0
+    gy[1:-1, :] = (inv[2:, :] - inv[:-2, :]) / 2.0
+    # smooth interiors only: the second differences of 1/d vanish on one plane
+    lap = np.full_like(inv, np.inf)
+    lap[1:-1, 1:-1] = np.abs(inv[1:-1, 2:] + inv[1:-1, :-2] - 2 * inv[1:-1, 1:-1]) + \
+        np.abs(inv[2:, 1:-1] + inv[:-2, 1:-1] - 2 * inv[1:-1, 1:-1])
+    hw = w.half_window
+    ys, xs = np.nonzero(lap < 1e-7)
+    keep = (xs > hw + 2) & (xs < w.width - hw - 3) & (ys > hw + 2) & (ys < w.height - hw - 3)
+    ys, xs = ys[keep], xs[keep]
+    g_u, g_v = gx[ys, xs] / ik00, gy[ys, xs] / ik11        # per unit of normalised coordinate
+    u = ik00 * (xs + 0.5) + ik02
+    v = ik11 * (ys + 0.5) + ik12
+    rho = 1.0 / (inv[ys, xs] - g_u * u - g_v * v)
+    slopes = np.stack([rho * g_u, rho * g_v], axis=1).astype(np.float32)
+    slanted = np.hypot(slopes[:, 0], slopes[:, 1]) > 0.25
+    assert slanted.sum() > 5000
+    xs, ys, slopes = xs[slanted], ys[slanted], slopes[slanted]
+    rng = np.random.default_rng(8)
+    pick = rng.choice(len(xs), 2000, replace=False)
+    xs, ys, slopes = xs[pick], ys[pick], slopes[pick]
+    depth = gt[ys, xs].astype(np.float32).astype(np.float64)
+    views = rng.integers(0, w.n_src, len(xs))
+    true = orc.ncc_plane_batch(xs, ys, views, depth, slopes, 1)
+    fronto = orc.ncc_plane_batch(xs, ys, views, depth, np.zeros_like(slopes), 1)
+    mirrored = orc.ncc_plane_batch(xs, ys, views, depth, -slopes, 1)
+    assert np.median(true) < np.median(fronto) < np.median(mirrored)
+    assert np.mean(true < mirrored) > 0.58
