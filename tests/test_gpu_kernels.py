@@ -298,7 +298,7 @@ def test_sweep_lockstep(small_scene, direction, sampler, parity_log):
 
 @pytest.mark.parametrize("sampler", [0, 1])
 def test_full_run_matches_oracle(small_scene, sampler, parity_log):
-    """The spec bar: at least 99.5% of final depths within 0.1% of the oracle's."""
+    """The end-to-end parity bar: at least 99.5% of final depths within 0.1% of the oracle's."""
     from patchmatch_cuda_gb300 import scene
     eng = make_engine(small_scene, sampler=sampler)
     orc = oracle_for(eng, small_scene)
