@@ -38,6 +38,8 @@ def test_default_params_mirror_main_cpp(engine_lib):
     assert (p.orientation_x, p.orientation_z) == (0.0, 1.0)  # main.cpp:72-76
     assert p.gpu_id == -1                                    # main.cpp:56-59
     assert p.quirks == 1 and p.prefilter == 0
+    # slanted planes per pixel are off: one normal for every pixel, as the reference runs
+    assert p.planes == 0 and abs(p.plane_depth_step - 0.02) < 1e-7 and abs(p.plane_slope_step - 0.25) < 1e-7
 
 
 def _views(n=3, w=32, h=24):
