@@ -270,17 +270,21 @@ pm_status pm_transpose_layers(const float *d_in, size_t in_pitch, float *d_out,
  * No counterpart in the reference: an addition for callers that cannot allocate device
  * memory (work recorded inside a stream capture that must not gain allocation nodes, hosts
  * whose framework owns every allocation, plugins that may only use the buffers they are
- * given). Same results as the box sums of pm_create's preparation (array2d_refImg.cu:11-67,
- * summed in double): for every pixel of a width x height float image in DEVICE memory, the
- * window sums S_I and S_II over the (2 half_window + 1)^2 window with zero border, and
- * c1 = S_II - S_I^2 / n over its n in-bounds pixels, clamped to 0 below 1e-5. Any output
- * pointer may be NULL. Intermediate row sums live in a fixed scratch array inside the library
- * (PM_NOALLOC_SCRATCH_DOUBLES doubles, 8 MiB, held on every device that loads the library
- * until the process exits); the image is processed in row strips that fit it, and a width
- * for which two rows plus the window's margin do not fit returns PM_ERR_SCRATCH_LIMIT. The
- * first call on a device resolves the scratch address (make it before any stream capture).
- * All calls on a device share the scratch: calls that overlap on the GPU race. Nothing is
- * allocated and the work is enqueued on `stream` (NULL: the default stream). */
+ * given). For every pixel of a width x height float image in DEVICE memory (row pitch
+ * ref_pitch bytes): the window sums S_I = sum I and S_II = sum I^2 over the
+ * (2 half_window + 1)^2 window centred on the pixel, pixels outside the image counting as
+ * zero, and c1 = S_II - S_I^2 / n with n the number of the window's pixels inside the image,
+ * set to 0 where it is below 1e-5. Sums are formed in double and stored as float, row-major
+ * with row pitch out_pitch bytes; any output pointer may be NULL. Both pitches must be
+ * multiples of 4 bytes and at least width * 4. Intermediate row sums live in a fixed scratch
+ * array inside the library (PM_NOALLOC_SCRATCH_DOUBLES doubles, 8 MiB, held on every device
+ * that loads the library until the process exits); the image is processed in row strips that
+ * fit it, and a width for which two rows plus the window's margin do not fit returns
+ * PM_ERR_SCRATCH_LIMIT. The first call on a device resolves the scratch address (make it
+ * before any stream capture); after cudaDeviceReset that address is stale, so do not call the
+ * entry point on a device that was reset. All calls on a device share the scratch: calls that
+ * overlap on the GPU race. Nothing is allocated and the work is enqueued on `stream` (NULL:
+ * the default stream). */
 #define PM_NOALLOC_SCRATCH_DOUBLES (1u << 20)
 pm_status pm_box_moments_noalloc(const float *d_ref, size_t ref_pitch, int width, int height,
                                  int half_window, float *d_sum_i, float *d_sum_ii, float *d_c1,

@@ -12,8 +12,10 @@
 // holds PM_NOALLOC_SCRATCH_DOUBLES doubles (8 MiB) until the process exits, whether or not the
 // entry point is called. Host code cannot use the array's name as a device address, so the
 // first call on each device (with that device current) resolves the address once with
-// cudaGetSymbolAddress; make that first call before any stream capture. Every call on a device
-// shares the one array, so calls whose work overlaps on the GPU (different streams, or
+// cudaGetSymbolAddress; make that first call before any stream capture. The address is kept
+// for the life of the process: after cudaDeviceReset the library's module may load at another
+// address, so the entry point must not be called on a device that was reset. Every call on a
+// device shares the one array, so calls whose work overlaps on the GPU (different streams, or
 // threads) race; serialise them. The row pass rewrites every scratch element the column pass
 // then reads, so nothing needs clearing between calls.
 #include <algorithm>
@@ -109,7 +111,8 @@ extern "C" pm_status pm_box_moments_noalloc(const float *d_ref, size_t ref_pitch
     if (!d_ref || width < 1 || height < 1 || (!d_sum_i && !d_sum_ii && !d_c1))
         return PM_ERR_INVALID_ARGUMENT;
     if (half_window < 1 || half_window > PM_MAX_HALF_WINDOW) return PM_ERR_WINDOW_SIZE;
-    if (ref_pitch < (size_t)width * sizeof(float) || out_pitch < (size_t)width * sizeof(float))
+    if (ref_pitch < (size_t)width * sizeof(float) || out_pitch < (size_t)width * sizeof(float) ||
+        ref_pitch % sizeof(float) != 0 || out_pitch % sizeof(float) != 0)
         return PM_ERR_INVALID_ARGUMENT;
     // One strip of image rows needs (rows + 2 * half_window) * width * 2 doubles of scratch;
     // at least two rows per strip must fit.
@@ -119,7 +122,10 @@ extern "C" pm_status pm_box_moments_noalloc(const float *d_ref, size_t ref_pitch
     double *scratch = nullptr;
     pm_status st = scratch_address(&scratch);
     if (st != PM_OK) return st;
-    const int strip = (int)std::min<size_t>((size_t)height, max_rows - 2 * (size_t)half_window);
+    // a strip's row pass launches (rows + 7) / 8 blocks along y, at most 65535
+    const size_t grid_rows = (size_t)65535 * 8 - 2 * (size_t)half_window;
+    const int strip = (int)std::min<size_t>(std::min<size_t>((size_t)height, max_rows - 2 * (size_t)half_window),
+                                            grid_rows);
     cudaStream_t s = (cudaStream_t)stream;
     const dim3 b(32, 8);
     for (int y0 = 0; y0 < height; y0 += strip) {

@@ -3,9 +3,12 @@ memory (for example work recorded into a stream capture that must not gain alloc
 a host framework that owns every allocation). The caller passes device buffers; the entry point
 keeps its intermediate row sums in a fixed scratch array inside the library.
 
-Checked against the engine's own preparation (pm_create then pm_get_ref_maps) on two calls in a
-row with different images and windows, so a stale scratch from the first call cannot hide an
-error in the second. This file is collected last on purpose.
+Checked against the engine's own preparation (pm_create then pm_get_ref_maps) on calls in a row
+with different images and windows, so a stale scratch from one call cannot hide an error in the
+next. The window sums are formed in the engine's order (zero rows add exactly 0.0), so S_I and
+S_II must equal the engine's bit for bit; c1 is checked against the oracle. One case is wide
+enough (8192 columns) that the image runs through several row strips of the fixed scratch, the
+last one short. This file is collected last on purpose.
 """
 import ctypes as C
 
@@ -27,7 +30,10 @@ def test_noalloc_moments_match_engine_on_two_calls():
     from oracle import pm_oracle
     from patchmatch_cuda_gb300 import Engine, _native
     lib = _native.load_engine()
-    cases = [(3, 320, 240, 5), (4, 200, 150, 9)]
+    # (seed, width, height, half-window): one strip each for the first two; the third needs
+    # 2^20 / (2 * 8192) = 64 strip rows of scratch per strip, so 46 image rows per strip and
+    # 5 strips, the last of 16 rows
+    cases = [(3, 320, 240, 5), (4, 200, 150, 9), (6, 8192, 200, 9), (3, 320, 240, 5)]
     for seed, width, height, hw in cases:
         w, sv = _views(seed, width, height)
         eng = Engine(sv.images, sv.ref_id, w.params(half_window=hw))
@@ -42,8 +48,8 @@ def test_noalloc_moments_match_engine_on_two_calls():
         assert st == 0, _native.STATUS_NAMES.get(st, st)
         torch.cuda.synchronize()
         got = out.cpu().numpy()
-        np.testing.assert_allclose(got[0], si, rtol=RTOL, atol=RTOL)
-        np.testing.assert_allclose(got[1], sii, rtol=RTOL, atol=RTOL)
+        np.testing.assert_array_equal(got[0], si)
+        np.testing.assert_array_equal(got[1], sii)
         osi, osii = pm_oracle.box_moments(ref, hw)
         xs = np.arange(width)
         ys = np.arange(height)
@@ -61,3 +67,13 @@ def test_noalloc_rejects_images_wider_than_its_scratch(engine_lib):
     st = limit.pm_box_moments_noalloc(C.c_void_p(16), width * 4, width, 4, 3, C.c_void_p(16), None, None,
                                       width * 4, None)
     assert _native.STATUS_NAMES[st] == "PM_ERR_SCRATCH_LIMIT"
+
+
+def test_noalloc_rejects_unaligned_pitches(engine_lib):
+    """Pitches that are not whole floats are refused before anything is launched."""
+    from patchmatch_cuda_gb300 import _native
+    lib = _native.load_engine()
+    for ref_pitch, out_pitch in [(64 * 4 + 2, 64 * 4), (64 * 4, 64 * 4 + 1), (63 * 4, 64 * 4)]:
+        st = lib.pm_box_moments_noalloc(C.c_void_p(16), ref_pitch, 64, 8, 3, C.c_void_p(16), None, None,
+                                        out_pitch, None)
+        assert _native.STATUS_NAMES[st] == "PM_ERR_INVALID_ARGUMENT"
