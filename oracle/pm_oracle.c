@@ -88,6 +88,13 @@ static inline real draw(const pmo_problem *p, int pixel, uint32_t sweep, int pur
                              ((uint32_t)purpose << 16) | (uint32_t)sub, p->batch_id);
 }
 
+/* Stream mode: the next draw of random state `state` (pmo_problem.rng_stream). */
+static inline real stream_draw(const pmo_problem *p, uint32_t state)
+{
+    const uint32_t k = p->rng_counts[state]++;
+    return (real)pmo_uniform(p->seed, state, k, PMO_STREAM_PURPOSE << 16, 0u);
+}
+
 /* A depth hypothesis U * (far - near) + near as the reference forms it: in float, the span
  * rounded to float first (array2d_wrapper.cu:15, patchMatch.cu:937), one fused multiply-add
  * (an exact float product fits a double, so rounding the double sum once is the fused result). */
@@ -673,7 +680,8 @@ void pmo_init_depth(const pmo_problem *p, double *depth)
     const int n = p->width * p->height;
     #pragma omp parallel for schedule(static)
     for (int i = 0; i < n; ++i) {
-        const float u = (float)draw(p, i, 0xFFFFFFFFu, PMO_RNG_INIT, 0);
+        const float u = p->rng_stream ? (float)stream_draw(p, (uint32_t)i)
+                                      : (float)draw(p, i, 0xFFFFFFFFu, PMO_RNG_INIT, 0);
         depth[i] = float_depth((double)(1.0f - u), p->depth_near, p->depth_far);
     }
 }
@@ -766,6 +774,7 @@ static long long sweep_impl(const pmo_problem *p, const double *sum_i, const dou
     const float d_hi = f_add(d_lo, (float)((double)(float)p->depth_far - (double)d_lo));
     if (line_begin < 0) line_begin = 0;
     if (line_end < 0 || line_end > nlines) line_end = nlines;
+    if (p->rng_stream && (planar || perturb > 0.0f || !p->rng_counts)) return -1;
     long long evals = 0;
 
     #pragma omp parallel reduction(+ : evals)
@@ -782,6 +791,9 @@ static long long sweep_impl(const pmo_problem *p, const double *sum_i, const dou
 #define COORD(k) (forward ? (k) : (nsteps - 1 - (k)))
 #define PX(k) (rotated ? COORD(k) : line)
 #define PY(k) (rotated ? line : COORD(k))
+            /* stream mode: the line's random state (the first pixel of its row or column) */
+            const uint32_t state = rotated ? (uint32_t)line * (uint32_t)W : (uint32_t)line;
+#define DRAW(pix, purpose, sub) (p->rng_stream ? stream_draw(p, state) : draw(p, pix, sweep_id, purpose, sub))
             /* 1. backward messages */
             for (int v = 0; v < V; ++v) beta[v] = (real)0.5;
             for (int k = nsteps - 1; k >= 0; --k) {
@@ -789,7 +801,7 @@ static long long sweep_impl(const pmo_problem *p, const double *sum_i, const dou
                 for (int v = 0; v < V; ++v) {
                     beta_all[(size_t)k * V + v] = beta[v];
                     real c = (real)cost[(size_t)pix * V + v];
-                    if (c == (real)2) c = draw(p, pix, sweep_id, PMO_RNG_BWD, v) * (real)2;
+                    if (c == (real)2) c = DRAW(pix, PMO_RNG_BWD, v) * (real)2;
                     beta[v] = msg_backward(beta[v], emission(c, a2), u_emit);
                 }
             }
@@ -798,7 +810,7 @@ static long long sweep_impl(const pmo_problem *p, const double *sum_i, const dou
                 int pix = PY(0) * W + PX(0);
                 for (int v = 0; v < V; ++v) {
                     real c = (real)cost[(size_t)pix * V + v];
-                    if (c == (real)2) c = draw(p, pix, sweep_id, PMO_RNG_FWD_POST, v) * (real)2;
+                    if (c == (real)2) c = DRAW(pix, PMO_RNG_FWD_POST, v) * (real)2;
                     alpha[v] = msg_forward((real)0.5, emission(c, a2), u_emit);
                 }
             }
@@ -819,7 +831,7 @@ static long long sweep_impl(const pmo_problem *p, const double *sum_i, const dou
                 for (int v = 0; v < V; ++v) {
                     real c = (real)cpix[v];
                     c_old[v] = c;
-                    if (c == (real)2) c = draw(p, pix, sweep_id, PMO_RNG_FWD_PRE, v) * (real)2;
+                    if (c == (real)2) c = DRAW(pix, PMO_RNG_FWD_PRE, v) * (real)2;
                     real a = msg_forward(alpha[v], emission(c, a2), u_emit);
                     real b = beta_all[(size_t)k * V + v];
                     real zn0 = a * b;
@@ -841,6 +853,7 @@ static long long sweep_impl(const pmo_problem *p, const double *sum_i, const dou
                     pmo_philox4x32_10(ctr, key, o);
                     float uw[4];
                     for (int k = 0; k < 4; ++k) uw[k] = (float)((o[k] >> 8) + 1u) * (1.0f / 16777216.0f);
+                    if (p->rng_stream) uw[0] = (float)stream_draw(p, state);  /* :937 */
                     const float u = uw[0], u2 = uw[1];
                     d_rand = (real)float_depth((double)u, p->depth_near, p->depth_far);
                     if (planar) {
@@ -885,7 +898,7 @@ static long long sweep_impl(const pmo_problem *p, const double *sum_i, const dou
                 real c3[3] = {0, 0, 0};
                 int tested = 0;
                 for (int j = 0; j < S; ++j) {
-                    real u = draw(p, pix, sweep_id, PMO_RNG_SAMPLE, j);
+                    real u = DRAW(pix, PMO_RNG_SAMPLE, j);
                     int view = -1;
                     for (int v = 0; v < V; ++v)
                         if (u <= cdf[v]) { view = v; break; }
@@ -921,7 +934,7 @@ static long long sweep_impl(const pmo_problem *p, const double *sum_i, const dou
                 }
                 for (int v = 0; v < V; ++v) {
                     real c = (real)cpix[v];
-                    if (c == (real)2) c = draw(p, pix, sweep_id, PMO_RNG_FWD_POST, v) * (real)2;
+                    if (c == (real)2) c = DRAW(pix, PMO_RNG_FWD_POST, v) * (real)2;
                     alpha[v] = msg_forward(alpha[v], emission(c, a2), u_emit);
                 }
                 if (view_sel)
@@ -932,6 +945,7 @@ static long long sweep_impl(const pmo_problem *p, const double *sum_i, const dou
 #undef COORD
 #undef PX
 #undef PY
+#undef DRAW
         }
         free(beta_all); free(beta); free(alpha); free(cdf); free(c_old); free(vsel);
     }

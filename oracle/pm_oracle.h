@@ -6,13 +6,16 @@
  * tests, the smoke entry point and the CPU-baseline legs of bench.py may load it. The
  * product path never calls it.
  *
- * Parity status: unpinned by the reference. yhsa678/patchMatch_cuda ships no tests,
- * fixtures or golden vectors, and its own code cannot be built here (it needs CUDA
- * texture references, which CUDA 12 removed, plus OpenCV and Boost). The restatement is
- * pinned instead by known-answer tests derived from the reference code (identical
- * windows -> 0, flat window -> 1, window outside the source -> 2, tie rule, message
- * fixed points, sampling of a one-hot CDF) and by the ground truth of seeded synthetic
- * scenes.
+ * Parity status: pinned to the reference's own code. yhsa678/patchMatch_cuda ships no tests,
+ * fixtures or golden vectors, and its CUDA build cannot run here (it needs CUDA texture
+ * references, which CUDA 12 removed, plus OpenCV and Boost); its device code does compile for
+ * the CPU (oracle/ref_host.cpp runs the kernels extracted unchanged by ref_extract.sh). That
+ * host run, with the reference's random states drawn as the stream mode below draws them,
+ * writes the golden vectors under tests/golden/ (ref_*.npz) that this restatement must
+ * reproduce: box sums, NCC, initial costs, messages, the tie rule, single sweeps in every
+ * direction and whole runs. Known-answer tests derived from the reference code (identical
+ * windows -> 0, flat window -> 1, window outside the source -> 2, tie rule, message fixed
+ * points) and the ground truth of seeded synthetic scenes add to that.
  *
  * Numbers: built with real = double (the FP64 oracle) or, with -DPMO_REAL_FLOAT, with
  * real = float (the timed CPU baseline). The API always passes double arrays.
@@ -78,7 +81,23 @@ typedef struct pmo_problem {
     float plane_depth_step;         /* planes: relative half-width of the local search's depth
                                        perturbation at sweep 0 (scaled by 2^(-sweep/4))      */
     float plane_slope_step;         /* planes: half-width of its slope perturbation at sweep 0 */
+    int rng_stream;                 /* 0: keyed draws (the engine's). 1: the reference's order
+                                       of draws from per-pixel random states (array2d_psng):
+                                       the initial depth of pixel i is the next draw of state i,
+                                       a sweep line draws from one state -- state x for
+                                       vertical sweeps over column x, state y*width for
+                                       horizontal sweeps over row y (patchMatch.cu:838-843,
+                                       :1034-1039) -- in the reference's order: backward
+                                       messages, the first step's forward message, then per
+                                       step the forward message, the random depth, the view
+                                       samples and the refreshed forward message. Draw k of
+                                       state s is Philox of counter (s, k, PMO_STREAM_PURPOSE
+                                       << 16, 0). Not with planes or perturbation.           */
+    uint32_t *rng_counts;           /* rng_stream: width*height draws made so far per state,
+                                       updated in place                                     */
 } pmo_problem;
+
+#define PMO_STREAM_PURPOSE 0x5EEDu
 
 /* Slanted-plane mode. A pixel's plane is its depth d (reference-camera z) and slopes (a, b):
  * normal n ~ (a, b, 1), so n . X = d s with the plane scale

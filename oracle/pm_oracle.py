@@ -1,9 +1,9 @@
 """ctypes wrapper of the CPU oracle (pm_oracle.c). TEST INFRASTRUCTURE ONLY.
 
 `Oracle(problem_inputs, fp32=False)` holds one problem: reference texels, source texels,
-homographies (double), K^-1 terms, parameters. Parity status: unpinned by the reference (it
-ships no tests or fixtures and cannot be built here); pinned by code-derived known-answer
-tests and synthetic ground truth.
+homographies (double), K^-1 terms, parameters. Parity status: pinned to the reference's own
+kernels run on the CPU (oracle/pm_ref.py, ref_host.cpp) through the golden vectors they wrote
+(tests/golden/ref_*.npz), plus code-derived known-answer tests and synthetic ground truth.
 """
 from __future__ import annotations
 
@@ -35,7 +35,7 @@ class _Problem(C.Structure):
         ("seed", C.c_uint64), ("batch_id", C.c_uint32), ("quirks", C.c_int),
         ("sampler", C.c_int), ("perturbation", C.c_float),
         ("planes", C.c_int), ("ee", C.c_void_p), ("plane_depth_step", C.c_float),
-        ("plane_slope_step", C.c_float),
+        ("plane_slope_step", C.c_float), ("rng_stream", C.c_int), ("rng_counts", C.c_void_p),
     ]
 
 # Slanted-plane mode's constants (pm_oracle.h)
@@ -321,6 +321,16 @@ class Oracle:
                                     self.sum_ii.ctypes.data, depth.ctypes.data, slopes.ctypes.data, cost.ctypes.data,
                                     vsel.ctypes.data)
         return depth, slopes, cost, vsel, n
+
+    def set_stream(self, counts: np.ndarray | None) -> None:
+        """Stream mode (the reference's order of draws from per-pixel random states) with the
+        uint32 (H, W) draw counts `counts`, updated in place by later calls; None: keyed draws."""
+        if counts is None:
+            self.p.rng_stream, self.p.rng_counts, self._counts = 0, None, None
+            return
+        assert counts.dtype == np.uint32 and counts.shape == (self.H, self.W) and counts.flags.c_contiguous
+        self._counts = counts
+        self.p.rng_stream, self.p.rng_counts = 1, counts.ctypes.data
 
     def run(self, iterations: int, num_samples: int):
         depth = np.empty((self.H, self.W), np.float64)

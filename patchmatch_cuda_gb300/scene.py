@@ -149,6 +149,29 @@ def make_views(w: Workload, seed: int | None = None) -> SceneViews:
     return SceneViews(images, ref_id, gt, w)
 
 
+def crop_reference(sv: SceneViews, x0: int, y0: int, width: int, height: int) -> SceneViews:
+    """The same cameras with the reference cut to the rectangle [x0, x0 + width) x
+    [y0, y0 + height): its principal point moves by (-x0, -y0), the sources stay whole. The
+    crop keeps the full image's pixel scale and texture, so a smaller problem has the same
+    statistics as the full one."""
+    ref = sv.images[sv.ref_id]
+    h, w = ref.image.shape
+    if not (0 <= x0 and 0 <= y0 and width > 0 and height > 0 and x0 + width <= w and y0 + height <= h):
+        raise ValueError("crop rectangle outside the reference image")
+    K = ref.K.astype(np.float64).copy()
+    K[0, 2] -= x0
+    K[1, 2] -= y0
+    crop = Image(K.astype(np.float32), ref.R, ref.T, np.ascontiguousarray(ref.image[y0:y0 + height, x0:x0 + width]))
+    images = list(sv.images)
+    images[sv.ref_id] = crop
+    wl = sv.workload
+    cw = Workload(f"{wl.name}_crop{width}x{height}", width, height, wl.n_src, wl.half_window, wl.iterations,
+                  wl.depth_near, wl.depth_far, wl.n_planes, wl.n_boxes, wl.prefilter, wl.gaussian_sigma,
+                  wl.sp_alpha, wl.seed, dict(wl.extra))
+    gt = np.ascontiguousarray(sv.gt_depth[y0:y0 + height, x0:x0 + width])
+    return SceneViews(images, sv.ref_id, gt, cw)
+
+
 BATCH_SIZES = [(640, 480), (1280, 720), (1920, 1080)]
 
 
