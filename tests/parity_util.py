@@ -51,3 +51,39 @@ def divergence_stats(prefix, nsteps):
 def view_selection_mismatches(gvs, ovs, mask):
     """Entries of the view-selection map (S, H, W) that differ on the masked pixels."""
     return int(np.sum(gvs[:, mask] != ovs[:, mask]))
+
+
+def special_value_flips(got, want):
+    """Costs where one side returned a special value of 1 - NCC (2: every source sample zero; 1:
+    a variance below the 1e-5 clamp) and the other did not. Those are jumps of the cost
+    function: a sample that lies a rounding step inside the source image in one precision and
+    outside in the other, or a variance a rounding step either side of the clamp."""
+    got, want = np.asarray(got, np.float64), np.asarray(want, np.float64)
+    special = np.isin(got, (1.0, 2.0)) | np.isin(want, (1.0, 2.0))
+    return special & (np.abs(got - want) > 0.25)
+
+
+def whole_run_lockstep(eng, orc, iterations, num_samples):
+    """Every sweep of a full schedule, the engine and the oracle each from the same state: the
+    oracle's trajectory (its initial depth and costs, then its own sweeps), rounded to float
+    where the engine takes it. Returns per-sweep (divergence events, decisions, cost errors
+    before each line's first divergence)."""
+    d = orc.init_depth()
+    c = orc.initial_costs(d)
+    rows = []
+    for it in range(iterations):
+        s = 1 if it == 0 else num_samples
+        for direction in range(4):
+            sid = 4 * it + direction
+            eng.set_depth(d.astype(np.float32))
+            eng.set_costs(c.astype(np.float32))
+            d = eng.depth().astype(np.float64)
+            c = eng.costs().astype(np.float64)
+            eng.run_sweep(direction, sid, s)
+            gd, gc = eng.depth(), eng.costs()
+            orc.sweep(d, c, direction, sid, s)
+            prefix, nsteps = first_divergence(gd, d, direction)
+            ev, dec = divergence_stats(prefix, nsteps)
+            mask = matched_mask(gd.shape, prefix, nsteps, direction)
+            rows.append((ev, dec, ncc_err(gc, c)[mask]))
+    return rows

@@ -49,9 +49,12 @@ def test_engine_matches_golden(golden, parity_log):
     eng.run()
     depth = eng.depth()
     rel = np.abs(depth - golden["depth"]) / golden["depth"]
+    # the last sweep's sampled views (usedImgsID): indices, equal wherever no line diverged before
+    vs_same = float(np.mean(np.all(eng.view_selection() == golden["view_sel"], axis=0)))
     parity_log("golden_plane3_128x96", ncc_err_max=float(err.max()), init_cost_err_max=float(cerr.max()),
-               depth_within_0p1pct=float(np.mean(rel <= 1e-3)))
+               depth_within_0p1pct=float(np.mean(rel <= 1e-3)), view_sel_equal=vs_same)
     assert err.max() <= 1e-4
     assert cerr.max() <= 1e-4
     assert np.mean(rel <= 1e-3) >= 0.99
+    assert vs_same >= 0.99
     eng.close()

@@ -11,7 +11,7 @@ beyond |cost| > 1) and 5e-4 at the 99.9th percentile for texture filtering; full
 import numpy as np
 import pytest
 
-from test_gpu_kernels import NCC_TOL, first_divergence, ncc_err
+from parity_util import NCC_TOL, first_divergence, ncc_err
 
 pytestmark = pytest.mark.gpu
 

@@ -1,0 +1,226 @@
+"""Parity at the benchmarked configuration (needs a GPU): box200_1280x720 -- 15x15 window
+(the reference's run<15>, patchMatch.cu:281), 10 source views, numOfSamples 5, depth [1, 20],
+no prefilter, u8 texels -- for both samplers.
+
+* NCC (patchMatch.cu:433-611) on the full 1280x720 reference, leading-edge, border and interior
+  windows, at ground-truth and random depths;
+* the initial costs (computeAllCostGivenDepth, patchMatch.cu:775-816) of all 9.2 M
+  (pixel, view) pairs;
+* one sweep in each direction (patchMatch.cu:818-1209) from the same state on bands of lines at
+  the image border and in the middle, with the sampled views (usedImgsID,
+  patchMatch.cu:1159-1163) compared index for index on every step before a line's first
+  divergence;
+* the full 5-iteration schedule on a 320x180 crop of the same reference (same cameras and
+  sources), small enough for the FP64 oracle: every sweep of it in lockstep from the oracle's
+  state, and the plain run end to end.
+
+Tolerances (costs: absolute in [0, 2], relative beyond). NCC 1e-4 at the 99.99th percentile for
+both samplers. Beyond it two kinds of values are expected at this size (9.2 M costs), and each
+has its own bound: (a) special-value flips, where one side returns 2 (every source sample zero)
+or 1 (a variance under the 1e-5 clamp) and the other does not -- a sample a rounding step either
+side of the source image's border -- at most 1e-6 of the costs; (b) low-variance windows far
+from the image origin, where FP32 source coordinates (a unit in the last place is 1.2e-4 pixel
+at x = 1200) move the samples enough to shift 1 - NCC by up to 5e-4 (2e-3 with the texture
+unit's 1/256 weights, whose steps the coordinates can cross) -- at most 2e-5 of the costs.
+Decisions: near-ties between FP32 and FP64 costs (argmin) or CDF values (view samples) flip
+now and then; the rate is bounded per decision, and the reference's own float code diverges
+from the same FP64 oracle at a similar rate (tests/test_ref_pin.py).
+"""
+import numpy as np
+import pytest
+
+from parity_util import (NCC_TOL, divergence_stats, first_divergence, matched_mask, ncc_err,
+                         special_value_flips, view_selection_mismatches, whole_run_lockstep)
+
+pytestmark = pytest.mark.gpu
+
+HW_TOL_Q999 = 5 * NCC_TOL
+HW_TOL_MAX = 20 * NCC_TOL
+
+
+@pytest.fixture(scope="module")
+def headline():
+    from patchmatch_cuda_gb300 import scene
+    return scene.make_views(scene.WORKLOADS["box200_1280x720"])
+
+
+@pytest.fixture(scope="module")
+def headline_crop(headline):
+    from patchmatch_cuda_gb300 import scene
+    return scene.crop_reference(headline, 480, 270, 320, 180)
+
+
+def make_engine(sv, **over):
+    from patchmatch_cuda_gb300 import Engine
+    return Engine(sv.images, sv.ref_id, sv.workload.params(**over))
+
+
+def oracle_for(eng, sv):
+    from oracle import pm_oracle
+    src = [eng.source_texels(v) for v in range(eng.n_src)]
+    ref, _, _ = eng.ref_maps()
+    return pm_oracle.from_images(sv.images, sv.ref_id, eng.params, source_texels=src, ref_texels=ref)
+
+
+def test_headline_parameters(headline):
+    """The workload is the benchmarked one: W = 15, V = 10, S = 5, 5 iterations, no prefilter."""
+    w = headline.workload
+    assert (w.width, w.height, w.n_src, 2 * w.half_window + 1, w.num_samples, w.iterations, w.prefilter) == \
+        (1280, 720, 10, 15, 5, 5, 0)
+
+
+@pytest.mark.parametrize("sampler", [0, 1])
+def test_headline_ncc(headline, sampler, parity_log):
+    eng = make_engine(headline, sampler=sampler)
+    orc = oracle_for(eng, headline)
+    w = headline.workload
+    rng = np.random.default_rng(15)
+    n = 8192
+    xs = rng.integers(0, w.width, n)
+    ys = rng.integers(0, w.height, n)
+    hw = w.half_window
+    xs[:512] = rng.integers(0, hw + 1, 512)                    # left edge (the quirk's leading edge)
+    ys[512:1024] = rng.integers(0, hw + 1, 512)                # top edge
+    xs[1024:1536] = rng.integers(w.width - hw - 1, w.width, 512)  # right edge
+    ys[1536:2048] = rng.integers(w.height - hw - 1, w.height, 512)  # bottom edge
+    vs = rng.integers(0, w.n_src, n)
+    gt = headline.gt_depth[ys, xs]
+    ds = np.where(rng.random(n) < 0.5, gt, rng.uniform(w.depth_near, w.depth_far, n)).astype(np.float32)
+    ax = rng.integers(0, 2, n)
+    err = ncc_err(eng.eval_costs(xs, ys, vs, ds, ax), orc.ncc_batch(xs, ys, vs, ds, ax))
+    parity_log(f"headline_ncc_sampler{sampler}", n=n, err_max=float(err.max()),
+               err_q999=float(np.quantile(err, 0.999)), err_median=float(np.median(err)),
+               err_max_edges=float(err[:2048].max()))
+    if sampler == 0:
+        assert err.max() <= NCC_TOL, f"max NCC error {err.max():.3g} at {np.argmax(err)}"
+    else:
+        assert np.quantile(err, 0.999) <= HW_TOL_Q999 and err.max() <= HW_TOL_MAX, err.max()
+    eng.close()
+
+
+@pytest.mark.parametrize("sampler", [0, 1])
+def test_headline_initial_costs(headline, sampler, parity_log):
+    eng = make_engine(headline, sampler=sampler)
+    orc = oracle_for(eng, headline)
+    eng.init_depth()
+    d = eng.depth()
+    np.testing.assert_allclose(d, orc.init_depth(), rtol=2e-7, atol=1e-6)
+    eng.compute_costs(1)
+    c = eng.costs()
+    oc = orc.initial_costs(d.astype(np.float64))
+    err = ncc_err(c, oc)
+    flips = special_value_flips(c, oc)
+    q = float(np.quantile(err, 0.9999))
+    rest = err[~flips]
+    parity_log(f"headline_initial_costs_sampler{sampler}", n=int(err.size), err_q9999=q,
+               special_value_flips=int(flips.sum()), err_max_other=float(rest.max()),
+               frac_over_1e4=float(np.mean(rest > NCC_TOL)))
+    assert q <= NCC_TOL, q
+    assert flips.sum() <= 1e-6 * err.size, int(flips.sum())
+    assert np.mean(rest > NCC_TOL) <= 2e-5
+    assert rest.max() <= (5 * NCC_TOL if sampler == 0 else HW_TOL_MAX), rest.max()
+    eng.close()
+
+
+def _bands(direction, w):
+    """A band at the image border (the first lines, whose windows are cut) and one in the
+    middle of the image, as ranges of sweep lines."""
+    n_lines = w.height if direction in (0, 2) else w.width
+    return [(0, 24), (n_lines // 2, n_lines // 2 + 24)]
+
+
+@pytest.mark.parametrize("sampler", [0, 1])
+@pytest.mark.parametrize("direction", [0, 1, 2, 3])
+def test_headline_sweep_lockstep(headline, direction, sampler, parity_log):
+    """One sweep with S = 5 from the engine's initial state, both sides recording the sampled
+    views. Before each line's first divergence (an argmin or CDF near-tie between FP32 and
+    FP64) every depth matches, every refreshed cost matches to the tolerance and the
+    view-selection map matches entry for entry but for CDF near-ties."""
+    w = headline.workload
+    S = w.num_samples
+    eng = make_engine(headline, sampler=sampler)
+    orc = oracle_for(eng, headline)
+    eng.init_depth()
+    eng.compute_costs(1)
+    d0 = eng.depth().astype(np.float64)
+    c0 = eng.costs().astype(np.float64)
+    eng.run_sweep(direction, 4 + direction, S, record_views=True)
+    gd, gc, gvs = eng.depth(), eng.costs(), eng.view_selection()
+    od, oc = d0.copy(), c0.copy()
+    ovs = np.full((S, w.height, w.width), 255, np.uint8)
+    events = decisions = 0
+    mask = np.zeros(gd.shape, bool)
+    for band in _bands(direction, w):
+        orc.sweep(od, oc, direction, 4 + direction, S, view_sel=ovs, lines=band)
+        prefix, nsteps = first_divergence(gd, od, direction, band)
+        e, dcs = divergence_stats(prefix, nsteps)
+        events += e
+        decisions += dcs
+        mask |= matched_mask(gd.shape, prefix, nsteps, direction, band[0])
+    cerr = ncc_err(gc, oc)[mask]
+    vs_bad = view_selection_mismatches(gvs, ovs, mask)
+    checked = int(S * mask.sum())
+    recorded = int(np.sum(ovs[:, mask] != 255))
+    parity_log(f"headline_sweep_lockstep_dir{direction}_sampler{sampler}", divergence_events=events,
+               decisions=decisions, matched_pixels=int(mask.sum()), cost_err_max=float(cerr.max()),
+               cost_err_q999=float(np.quantile(cerr, 0.999)), view_sel_checked=checked,
+               view_sel_recorded=recorded, view_sel_mismatches=vs_bad)
+    assert events / decisions <= 5e-4, f"{events} divergences in {decisions} decisions"
+    assert np.quantile(cerr, 0.999) <= NCC_TOL and cerr.max() <= 5 * NCC_TOL, cerr.max()
+    assert recorded > 0.5 * checked
+    # view samples are indices: equal but for CDF near-ties (a uniform within a rounding step of
+    # a CDF value), which leave the depth decision unchanged
+    assert vs_bad <= 5e-5 * checked, f"{vs_bad} of {checked} view-selection entries differ before divergence"
+    eng.close()
+
+
+@pytest.mark.parametrize("sampler", [0, 1])
+def test_headline_whole_run_lockstep(headline_crop, sampler, parity_log):
+    """All 20 sweeps of the benchmarked schedule (S = 1 in the first iteration), each from the
+    oracle's state: decisions equal but for near-ties, at most 1e-4 per decision, and every cost
+    before a line's first divergence within the NCC bounds."""
+    sv = headline_crop
+    w = sv.workload
+    eng = make_engine(sv, sampler=sampler)
+    orc = oracle_for(eng, sv)
+    rows = whole_run_lockstep(eng, orc, w.iterations, w.num_samples)
+    events = sum(r[0] for r in rows)
+    decisions = sum(r[1] for r in rows)
+    cerr = np.concatenate([r[2] for r in rows])
+    parity_log(f"headline_whole_run_lockstep_crop320x180_sampler{sampler}", divergence_events=events,
+               decisions=decisions, per_sweep_events=[r[0] for r in rows], cost_err_q9999=float(np.quantile(cerr, 0.9999)),
+               cost_err_max=float(cerr.max()))
+    assert events <= 1e-4 * decisions, f"{events} divergences in {decisions} decisions"
+    assert np.quantile(cerr, 0.9999) <= NCC_TOL
+    assert cerr.max() <= (5 * NCC_TOL if sampler == 0 else HW_TOL_MAX), cerr.max()
+    eng.close()
+
+
+@pytest.mark.parametrize("sampler", [0, 1])
+def test_headline_full_run(headline_crop, sampler, parity_log):
+    """The plain 5-iteration run end to end against the FP64 oracle's. Over 20 sweeps each
+    near-tie (above) changes the random draws a region keeps, so the two maps converge on the
+    same surfaces with depths a fraction of a percent apart there: at least 99 % of the depths
+    agree within 1 % and 90 % within 0.1 %, the bad-pixel rates within half a point, and the
+    last sweep's view selection on at least 95 % of the pixels."""
+    from patchmatch_cuda_gb300 import scene
+    sv = headline_crop
+    w = sv.workload
+    eng = make_engine(sv, sampler=sampler)
+    orc = oracle_for(eng, sv)
+    eng.run()
+    gd, gvs = eng.depth(), eng.view_selection()
+    od, _, ovs, _ = orc.run(w.iterations, w.num_samples)
+    rel = np.abs(gd - od) / od
+    within_01, within_1 = float(np.mean(rel <= 1e-3)), float(np.mean(rel <= 1e-2))
+    vs_same = float(np.mean(np.all(gvs == ovs, axis=0)))
+    bad_g = scene.bad_pixel_rate(gd, sv.gt_depth)
+    bad_o = scene.bad_pixel_rate(od.astype(np.float32), sv.gt_depth)
+    parity_log(f"headline_full_run_crop320x180_sampler{sampler}", within_0p1pct=within_01, within_1pct=within_1,
+               bit_identical=float(np.mean(gd == od.astype(np.float32))), view_sel_equal=vs_same,
+               bad1_gpu=bad_g, bad1_oracle=bad_o)
+    assert within_1 >= 0.99 and within_01 >= 0.90, (within_1, within_01)
+    assert abs(bad_g - bad_o) <= 0.005, (bad_g, bad_o)
+    assert vs_same >= 0.95, vs_same
+    assert np.all((gvs < w.n_src) | (gvs == 255))  # 255: no view drawn (or the line's first step)
+    eng.close()

@@ -8,15 +8,10 @@ misaligned pairing of reference and source samples lets 1 - NCC leave [0, 2]); b
 import numpy as np
 import pytest
 
+from parity_util import (NCC_TOL, divergence_stats, first_divergence, matched_mask, ncc_err,  # noqa: F401
+                         view_selection_mismatches)
+
 pytestmark = pytest.mark.gpu
-
-
-NCC_TOL = 1e-4
-
-
-def ncc_err(got, want):
-    """Error in units of the tolerance: absolute within [0, 2], relative beyond."""
-    return np.abs(np.asarray(got, np.float64) - want) / np.maximum(1.0, np.abs(want))
 
 
 def bilinear_ref(img, xs, ys):
@@ -241,20 +236,6 @@ def test_initial_depth_and_costs_match_oracle(small_scene, parity_log):
     eng.close()
 
 
-def first_divergence(gd, od, direction):
-    """Per line of the sweep, the number of leading steps (in processing order) whose depth
-    decision matches the oracle's."""
-    same = np.abs(gd - od) <= 1e-6 * np.abs(od)
-    if direction in (0, 2):       # horizontal sweeps: lines are rows
-        lines = same
-    else:                         # vertical sweeps: lines are columns
-        lines = same.T
-    if direction in (2, 3):       # processed from the far end
-        lines = lines[:, ::-1]
-    prefix = np.where(lines.all(axis=1), lines.shape[1], np.argmin(lines, axis=1))
-    return prefix, lines.shape[1]
-
-
 @pytest.mark.parametrize("sampler", [0, 1])
 @pytest.mark.parametrize("direction", [0, 1, 2, 3])
 def test_sweep_lockstep(small_scene, direction, sampler, parity_log):
@@ -269,30 +250,28 @@ def test_sweep_lockstep(small_scene, direction, sampler, parity_log):
     d0 = eng.depth().astype(np.float64)
     c0 = eng.costs().astype(np.float64)
     S = small_scene.workload.num_samples
-    eng.run_sweep(direction, 4 + direction, S)
-    gd, gc = eng.depth(), eng.costs()
+    eng.run_sweep(direction, 4 + direction, S, record_views=True)
+    gd, gc, gvs = eng.depth(), eng.costs(), eng.view_selection()
     od, oc = d0.copy(), c0.copy()
-    orc.sweep(od, oc, direction, 4 + direction, S)
+    ovs = np.full(gvs.shape, 255, np.uint8)
+    orc.sweep(od, oc, direction, 4 + direction, S, view_sel=ovs)
     prefix, nsteps = first_divergence(gd, od, direction)
-    events = int(np.sum(prefix < nsteps))
-    decisions = int(np.sum(np.minimum(prefix + 1, nsteps)))
+    events, decisions = divergence_stats(prefix, nsteps)
     rate = events / decisions
-    mask = np.zeros(gd.shape, bool)
-    for line, p in enumerate(prefix):
-        steps = np.arange(p)
-        if direction in (2, 3):
-            steps = nsteps - 1 - steps
-        if direction in (0, 2):
-            mask[line, steps] = True
-        else:
-            mask[steps, line] = True
+    mask = matched_mask(gd.shape, prefix, nsteps, direction)
     cerr = ncc_err(gc, oc)[mask]
+    vs_bad = view_selection_mismatches(gvs, ovs, mask)
     parity_log(f"sweep_lockstep_dir{direction}_sampler{sampler}", divergence_events=events, decisions=decisions,
                divergence_rate=rate, matched_fraction=float(mask.mean()),
-               cost_err_max=float(cerr.max()), cost_err_q999=float(np.quantile(cerr, 0.999)))
+               cost_err_max=float(cerr.max()), cost_err_q999=float(np.quantile(cerr, 0.999)),
+               view_sel_checked=int(S * mask.sum()), view_sel_mismatches=vs_bad)
     tol = NCC_TOL if sampler == 0 else 5 * NCC_TOL
     assert rate <= 2e-4, f"{events} divergences in {decisions} decisions"
     assert cerr.max() <= tol, f"cost error {cerr.max():.3g} before divergence"
+    # the sampled views (usedImgsID, patchMatch.cu:1159-1163) are indices: equal entry for entry
+    # but for CDF near-ties (a uniform within a rounding step of a CDF value), which leave the
+    # decision unchanged
+    assert vs_bad <= 5e-5 * S * mask.sum(), f"{vs_bad} view-selection entries differ before divergence"
     eng.close()
 
 
@@ -310,9 +289,14 @@ def test_full_run_matches_oracle(small_scene, sampler, parity_log):
     frac = float(np.mean(rel <= 1e-3))
     bad_g = scene.bad_pixel_rate(gd, small_scene.gt_depth)
     bad_o = scene.bad_pixel_rate(od.astype(np.float32), small_scene.gt_depth)
-    parity_log(f"full_run_plane3_320x240_sampler{sampler}", within_0p1pct=frac, bad1_gpu=bad_g, bad1_oracle=bad_o)
+    # the last sweep's sampled views: equal wherever the lines did not diverge before
+    gvs = eng.view_selection()
+    vs_same = float(np.mean(np.all(gvs == ovs, axis=0)))
+    parity_log(f"full_run_plane3_320x240_sampler{sampler}", within_0p1pct=frac, bad1_gpu=bad_g, bad1_oracle=bad_o,
+               view_sel_equal=vs_same)
     assert abs(bad_g - bad_o) <= 0.01, (bad_g, bad_o)
     assert frac >= 0.995, f"only {frac:.4f} of depths within 0.1% of the oracle"
+    assert vs_same >= 0.99, f"view selection equal on only {vs_same:.4f} of the pixels"
     st = eng.stats()
     assert st.cost_evals > 0
     eng.close()
@@ -335,8 +319,7 @@ def test_sweep_lockstep_local_search(small_scene, direction, parity_log):
     od, oc = d0.copy(), c0.copy()
     orc.sweep(od, oc, direction, 4 + direction, S)
     prefix, nsteps = first_divergence(gd, od, direction)
-    events = int(np.sum(prefix < nsteps))
-    decisions = int(np.sum(np.minimum(prefix + 1, nsteps)))
+    events, decisions = divergence_stats(prefix, nsteps)
     changed = float(np.mean(np.abs(gd - d0) > 1e-6 * d0))
     parity_log(f"sweep_lockstep_local_search_dir{direction}", divergence_events=events, decisions=decisions,
                changed_fraction=changed)

@@ -9,7 +9,7 @@ the tolerances of the reference-mode tests (1e-4 exact sampler, 5e-4 texture fil
 import numpy as np
 import pytest
 
-from test_gpu_kernels import NCC_TOL, first_divergence, ncc_err
+from parity_util import NCC_TOL, first_divergence, ncc_err
 
 pytestmark = pytest.mark.gpu
 
