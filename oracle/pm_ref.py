@@ -1,10 +1,13 @@
 """ctypes wrapper of the reference's own kernels run on the CPU (ref_host.cpp). TEST
-INFRASTRUCTURE ONLY: it pins the oracle (pm_oracle.c) to the reference's code and writes the
-golden vectors under tests/golden/ (make_ref_golden.py).
+INFRASTRUCTURE ONLY: it pins the oracle (pm_oracle.c) to the reference's code, writes the
+golden vectors under tests/golden/ (make_ref_golden.py) and is bench.py's CPU baseline.
 
-The libraries are built from the reference's sources (`make -C oracle ref`, ref_extract.sh), so
-they exist only where those sources are; elsewhere `available()` is False and the committed
-golden vectors stand in for them.
+The libraries are built from the reference's sources (`make -C oracle ref`, ref_extract.sh) or,
+where the sources are absent, from the kernels ref_extract.sh already copied out of them into
+oracle/_ref/ref_kernels.inc (`make -C oracle ref-libs`; the file is not committed, it travels
+with a working tree). Where neither is present `available()` is False and the committed golden
+vectors stand in for them. bench.py times this build (the reference's own code) as its CPU
+baseline where it is available.
 
     lib = load(wide)        wide=False: the reference as written (float arithmetic);
                             wide=True: the same code with its floats widened to double.
@@ -44,15 +47,23 @@ def sources_present() -> bool:
 
 
 def build() -> None:
-    """Builds oracle/_ref from the reference's sources (only where they are present)."""
-    r = subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF_ROOT={REFERENCE_ROOT}"],
+    """Builds oracle/_ref from the reference's sources, or, where they are absent, from the
+    kernels already extracted from them into oracle/_ref."""
+    target = "ref" if sources_present() else "ref-libs"
+    r = subprocess.run(["make", "-s", "-C", str(HERE), target, f"REF_ROOT={REFERENCE_ROOT}"],
                        capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"reference build failed:\n{r.stdout}\n{r.stderr}")
 
 
+def extracted_present() -> bool:
+    """The reference's kernels extracted from its sources (ref_kernels.inc) are here: the
+    libraries can be built even where the sources are not."""
+    return (REF_OUT / "ref_kernels.inc").exists()
+
+
 def available() -> bool:
-    return (REF_OUT / "libpm_ref_f64.so").exists() or sources_present()
+    return sources_present() or extracted_present()
 
 
 _libs: dict[bool, C.CDLL] = {}
@@ -71,7 +82,7 @@ def load(wide: bool = False) -> C.CDLL:
     lib.pmr_init_depth.argtypes = [P, P, P]
     lib.pmr_initial_costs.argtypes = [P, P, P]
     lib.pmr_sweep.restype = C.c_longlong
-    lib.pmr_sweep.argtypes = [P, C.c_int, C.c_int, P, P, P, P]
+    lib.pmr_sweep.argtypes = [P, C.c_int, C.c_int, P, P, P, P, C.c_int, C.c_int, P, P]
     lib.pmr_run.restype = C.c_longlong
     lib.pmr_run.argtypes = [P, C.c_int, C.c_int, P, P, P]
     lib.pmr_ncc.argtypes = [P, C.c_int, P, P, P, P, P, P]
@@ -148,16 +159,20 @@ class RefProblem:
         assert self.lib.pmr_initial_costs(self._pp, depth.ctypes.data, c.ctypes.data) == 0
         return c
 
-    def sweep(self, depth, cost, counts, direction, num_samples, view_sel=None) -> int:
+    def sweep(self, depth, cost, counts, direction, num_samples, view_sel=None, lines=(0, -1),
+              with_evals=False):
         """In place on float64 depth (H, W), cost (H, W, V) and uint32 counts (H, W); returns
-        the homography-table fetches outside the table (samples that found no view)."""
+        the homography-table fetches outside the table (samples that found no view), and with
+        with_evals also the number of NCC evaluations and the kernel launch's wall time in
+        seconds. Only the reference's blocks of 32 lines that hold `lines` run."""
         for a, t in ((depth, np.float64), (cost, np.float64), (counts, np.uint32)):
             assert a.dtype == t and a.flags.c_contiguous
         vs = view_sel.ctypes.data if view_sel is not None else None
+        ev, sec = C.c_longlong(0), C.c_double(0.0)
         n = self.lib.pmr_sweep(self._pp, direction, num_samples, depth.ctypes.data, cost.ctypes.data,
-                               counts.ctypes.data, vs)
+                               counts.ctypes.data, vs, lines[0], lines[1], C.byref(ev), C.byref(sec))
         assert n >= 0
-        return n
+        return (n, ev.value, sec.value) if with_evals else n
 
     def run(self, iterations, num_samples):
         depth = np.empty((self.H, self.W), np.float64)

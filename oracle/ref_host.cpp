@@ -27,11 +27,14 @@
 #endif
 
 #include <algorithm>
+#include <atomic>
 #include <barrier>
+#include <chrono>
 #include <thread>
 #include <vector>
 
 thread_local pmr_dim3 threadIdx, blockIdx;
+thread_local unsigned long long pmr_point_fetches = 0, pmr_point_outside = 0;
 pmr_dim3 blockDim, gridDim;
 uint64_t pmr_seed;
 alignas(64) unsigned char pmr_dynamic_shared[1 << 18];
@@ -77,15 +80,23 @@ namespace {
 
 constexpr int BLOCK = 32;  // N of patchMatch.cu:37: the reference's block width
 
-// Runs `blocks` blocks of BLOCK host threads, one block at a time.
+// Point fetches (homography-table reads) of the last launch, summed over its threads, and the
+// launch's wall time.
+std::atomic<unsigned long long> g_fetches{0}, g_outside{0};
+double g_launch_seconds = 0.0;
+
+// Runs blocks [b0, b1) of a grid of `blocks` blocks of BLOCK host threads, one block at a time.
 template <class F>
-void launch_lines(int blocks, F &&kernel)
+void launch_lines(int blocks, F &&kernel, int b0 = 0, int b1 = -1)
 {
     blockDim = {BLOCK, 1, 1};
     gridDim = {(unsigned)blocks, 1, 1};
+    g_fetches = 0;
+    g_outside = 0;
     std::barrier<> bar(BLOCK);
     g_barrier = &bar;
-    for (int b = 0; b < blocks; ++b) {
+    const auto t0 = std::chrono::steady_clock::now();
+    for (int b = b0; b < (b1 < 0 ? blocks : std::min(b1, blocks)); ++b) {
         std::vector<std::thread> th;
         th.reserve(BLOCK);
         for (int t = 0; t < BLOCK; ++t)
@@ -93,10 +104,14 @@ void launch_lines(int blocks, F &&kernel)
                 if (!PMR_WIDE) flush_denormals();
                 threadIdx = {(unsigned)t, 0, 0};
                 blockIdx = {(unsigned)b, 0, 0};
+                pmr_point_fetches = pmr_point_outside = 0;
                 kernel();
+                g_fetches += pmr_point_fetches;
+                g_outside += pmr_point_outside;
             });
         for (auto &x : th) x.join();
     }
+    g_launch_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     g_barrier = nullptr;
 }
 
@@ -212,7 +227,6 @@ struct Device {
         allImgsTexture.layers = p->n_src;
         allImgsTexture.filterMode = cudaFilterModeLinear;
         allImgsTexture.fixed_point_weights = p->fixed_point_weights;
-        allImgsTexture.outside_rows = 0;
         refImgTexture.data = p->ref;
         refImgTexture.width = p->width;
         refImgTexture.height = p->height;
@@ -225,7 +239,6 @@ struct Device {
         transformTexture.height = p->n_src;
         transformTexture.layers = 1;
         transformTexture.filterMode = cudaFilterModePoint;
-        transformTexture.outside_rows = 0;
         orientation[0] = (PR)p->orientation[0];
         orientation[1] = (PR)p->orientation[1];
         orientation[2] = (PR)p->orientation[2];
@@ -314,7 +327,7 @@ void initial_costs_w(Device &dev, Pitched<PR> &depth_t, Pitched<PR> &cost_t)
 // depth and cost maps.
 template <int WS>
 void sweep_w(Device &dev, int dir, int S, Pitched<PR> &depth, Pitched<PR> &cost, std::vector<curandState> &rs,
-             uint8_t *view_sel)
+             uint8_t *view_sel, int line_begin, int line_end)
 {
     const pmr_problem *p = dev.p;
     const bool rotated = dir == 0 || dir == 2;
@@ -338,6 +351,8 @@ void sweep_w(Device &dev, int dir, int S, Pitched<PR> &depth, Pitched<PR> &cost,
         used.init(w, h, S);
         std::fill(used.begin(), used.end(), (uint8_t)255);
     }
+    const int b0 = std::max(0, line_begin) / BLOCK;
+    const int b1 = line_end < 0 ? -1 : (std::min(line_end, w) + BLOCK - 1) / BLOCK;
     launch_lines((w - 1) / BLOCK + 1, [&] {
         if (down)
             topToDown<WS>(c.ptr(), ri.ptr(), si.ptr(), sii.ptr(), si.pitch(), w, h, d.ptr(), d.pitch(), spmap.ptr(),
@@ -348,7 +363,7 @@ void sweep_w(Device &dev, int dir, int S, Pitched<PR> &depth, Pitched<PR> &cost,
                           spmap.pitch(), S, rs.data(), state_pitch, (PR)p->depth_near, (PR)p->depth_far,
                           p->half_window, rotated, (unsigned)V, a2, view_sel ? used.ptr() : nullptr,
                           view_sel ? used.pitch() : 0);
-    });
+    }, b0, b1);
     if (rotated) {
         transpose(d_t, depth);
         transpose(c_t, cost);
@@ -446,10 +461,13 @@ int pmr_initial_costs(const pmr_problem *p, const double *depth, double *cost)
 /* One sweep in direction dir (0 left-to-right, 1 top-to-bottom, 2 right-to-left, 3
  * bottom-to-top) with S view samples, in place on depth and pixel-major costs; counts[] are
  * the per-pixel random states' draw counts (updated). view_sel (S x height x width, written
- * only by bottom-to-top sweeps, as the reference records usedImgsID) may be NULL. Returns the
- * number of homography-table fetches outside the table (view samples that found no view). */
+ * only by bottom-to-top sweeps, as the reference records usedImgsID) may be NULL. Only the
+ * blocks of 32 lines that hold lines [line_begin, line_end) run (line_end < 0: all). Returns
+ * the number of homography-table fetches outside the table (view samples that found no view);
+ * *evals (if not NULL) receives the number of computeNCC calls and *seconds the wall time of
+ * the kernel launch alone (not the host's layout conversions around it). */
 long long pmr_sweep(const pmr_problem *p, int dir, int S, double *depth, double *cost, uint32_t *counts,
-                    uint8_t *view_sel)
+                    uint8_t *view_sel, int line_begin, int line_end, long long *evals, double *seconds)
 {
     if (!supported(p) || dir < 0 || dir > 3 || S < 1) return -1;
     Device dev(p);
@@ -458,7 +476,7 @@ long long pmr_sweep(const pmr_problem *p, int dir, int S, double *depth, double 
     costs_to_layers(cost, p->width, p->height, p->n_src, c);
     uint8_t *vs = dir == 3 ? view_sel : nullptr;
     switch (2 * p->half_window + 1) {
-#define X(n) case n: sweep_w<n>(dev, dir, S, d, c, rs, vs); break;
+#define X(n) case n: sweep_w<n>(dev, dir, S, d, c, rs, vs, line_begin, line_end); break;
         PMR_W_CASES(X)
 #undef X
     default: return -1;
@@ -466,7 +484,9 @@ long long pmr_sweep(const pmr_problem *p, int dir, int S, double *depth, double 
     for (size_t i = 0; i < d.size(); ++i) depth[i] = (double)d[i];
     layers_to_costs(c, cost);
     store_counts(rs, counts);
-    return (long long)transformTexture.outside_rows.load();
+    if (evals) *evals = (long long)(g_fetches.load() / 18);
+    if (seconds) *seconds = g_launch_seconds;
+    return (long long)g_outside.load();
 }
 
 /* PatchMatch::run<W> (patchMatch.cu:307-394) from the random initial depth: iteration 0
@@ -483,7 +503,7 @@ long long pmr_run(const pmr_problem *p, int iterations, int S, double *depth, do
     for (int it = 0; it < iterations; ++it)
         for (int dir = 0; dir < 4; ++dir) {
             const long long o = pmr_sweep(p, dir, it == 0 ? 1 : S, depth, cost, counts.data(),
-                                          it == iterations - 1 ? view_sel : nullptr);
+                                          it == iterations - 1 ? view_sel : nullptr, 0, -1, nullptr, nullptr);
             if (o < 0) return -1;
             outside += o;
         }

@@ -34,7 +34,6 @@
 #include <stdint.h>
 #include <string.h>
 
-#include <atomic>
 
 #ifndef PMR_REAL
 #define PMR_REAL float
@@ -70,7 +69,6 @@ struct texture {
     cudaTextureFilterMode filterMode = cudaFilterModePoint;
     int normalized = 0;
     int fixed_point_weights = 0;                 /* linear filtering: 1/256 weights */
-    mutable std::atomic<unsigned long long> outside_rows{0};  /* point fetches outside the rows */
 };
 
 template <class T, int type, cudaTextureReadMode mode>
@@ -84,17 +82,23 @@ static inline pmr_real pmr_texel(const texture<T, type, mode> &t, int x, int y, 
 
 static inline pmr_real pmr_q8(pmr_real f) { return (pmr_real)floor((double)f * 256.0 + 0.5) / (pmr_real)256; }
 
+/* Point fetches made by this host thread (only the homography table is point-filtered: 18
+ * per computeNCC call, so their count / 18 is the number of NCC evaluations), and those
+ * outside the table's rows. */
+extern thread_local unsigned long long pmr_point_fetches, pmr_point_outside;
+
 template <class T, int type, cudaTextureReadMode mode>
 static pmr_real tex2DLayered(const texture<T, type, mode> &t, pmr_real x, pmr_real y, int layer)
 {
+    if (t.filterMode == cudaFilterModePoint) ++pmr_point_fetches;
     if (!isfinite((double)x) || !isfinite((double)y)) {
-        if (t.filterMode == cudaFilterModePoint) t.outside_rows++;
+        if (t.filterMode == cudaFilterModePoint) ++pmr_point_outside;
         return (pmr_real)0;
     }
     layer = layer < 0 ? 0 : (layer >= t.layers ? t.layers - 1 : layer);
     if (t.filterMode == cudaFilterModePoint) {
         const double fx = floor((double)x), fy = floor((double)y);
-        if (fy < 0.0 || fy >= (double)t.height) t.outside_rows++;
+        if (fy < 0.0 || fy >= (double)t.height) ++pmr_point_outside;
         if (fx < 0.0 || fy < 0.0 || fx >= (double)t.width || fy >= (double)t.height) return (pmr_real)0;
         return pmr_texel(t, (int)fx, (int)fy, layer);
     }
