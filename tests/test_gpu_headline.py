@@ -224,3 +224,34 @@ def test_headline_full_run(headline_crop, sampler, parity_log):
     assert vs_same >= 0.95, vs_same
     assert np.all((gvs < w.n_src) | (gvs == 255))  # 255: no view drawn (or the line's first step)
     eng.close()
+
+
+@pytest.mark.parametrize("texels", ["f32", "f16"])
+def test_headline_texel_precision(headline, texels, parity_log):
+    """The benchmarked workload with the box prefilter (GaussianBlurCUDA as written), so that
+    texels are no longer 8-bit: the engine's NCC with FP32 texels (precision fp32) and with FP16
+    texels (precision mixed) against the FP64 oracle on texels prefiltered in FP64 and rounded
+    to float -- the accuracy the FP16 storage costs. Window moments are accumulated shifted by
+    each column's first sample in FP32 in both cases (the engine's replacement for compensated
+    sums); the reference-window terms come from an FP64 preparation pass."""
+    from oracle import pm_oracle
+    eng = make_engine(headline, prefilter=1, sampler=0, precision=0 if texels == "f32" else 1)
+    assert eng.stats().texel_bytes == (4 if texels == "f32" else 2)
+    orc = pm_oracle.from_images(headline.images, headline.ref_id, eng.params)  # its own texels
+    w = headline.workload
+    rng = np.random.default_rng(16)
+    n = 8192
+    xs, ys = rng.integers(0, w.width, n), rng.integers(0, w.height, n)
+    vs = rng.integers(0, w.n_src, n)
+    gt = headline.gt_depth[ys, xs]
+    ds = np.where(rng.random(n) < 0.5, gt, rng.uniform(w.depth_near, w.depth_far, n)).astype(np.float32)
+    ax = rng.integers(0, 2, n)
+    err = ncc_err(eng.eval_costs(xs, ys, vs, ds, ax), orc.ncc_batch(xs, ys, vs, ds, ax))
+    parity_log(f"headline_box_prefilter_texels_{texels}", n=n, err_max=float(err.max()),
+               err_q999=float(np.quantile(err, 0.999)), err_q99=float(np.quantile(err, 0.99)),
+               err_median=float(np.median(err)))
+    if texels == "f32":
+        assert np.quantile(err, 0.999) <= NCC_TOL and err.max() <= 5 * NCC_TOL
+    else:  # FP16 keeps 11 significant bits of each texel: about 2.4e-4 relative
+        assert np.quantile(err, 0.99) <= 10 * NCC_TOL and err.max() <= 100 * NCC_TOL
+    eng.close()
