@@ -87,3 +87,32 @@ def whole_run_lockstep(eng, orc, iterations, num_samples):
             mask = matched_mask(gd.shape, prefix, nsteps, direction)
             rows.append((ev, dec, ncc_err(gc, c)[mask]))
     return rows
+
+
+def oracle_schedule(orc, depth, cost, iterations, num_samples):
+    """The reference's schedule (pmo_run's sweeps) from a given state; in place, returns depth."""
+    for it in range(iterations):
+        s = 1 if it == 0 else num_samples
+        for direction in range(4):
+            orc.sweep(depth, cost, direction, 4 * it + direction, s)
+    return depth
+
+
+def agreement(a, b):
+    """Shares of pixels whose depths agree within 0.1 % and within 1 %."""
+    rel = np.abs(np.asarray(a, np.float64) - b) / np.asarray(b, np.float64)
+    return float(np.mean(rel <= 1e-3)), float(np.mean(rel <= 1e-2))
+
+
+def float_floor(eng, sv, od, iterations, num_samples):
+    """The oracle's own FP32 build (pm_oracle.c with real = float: the same rules in float, on the
+    engine's texels) run over the same schedule, and its agreement (within 0.1 %, within 1 %)
+    with the FP64 oracle's depths `od`. Over 20 sweeps a near-tie anywhere changes which random
+    draws a region keeps, so this is the agreement a float implementation of the rules reaches;
+    it varies widely from scene to scene (85-98 % within 0.1 % on the crops tested)."""
+    from oracle import pm_oracle
+    src = [eng.source_texels(v) for v in range(eng.n_src)]
+    ref, _, _ = eng.ref_maps()
+    o32 = pm_oracle.from_images(sv.images, sv.ref_id, eng.params, source_texels=src, ref_texels=ref, fp32=True)
+    d32 = o32.run(iterations, num_samples)[0]
+    return agreement(d32, od)
