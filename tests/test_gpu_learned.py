@@ -268,37 +268,41 @@ def test_run_requires_an_attached_network(small_views):
 
 
 def test_learned_schedule_against_random_controls(parity_log):
-    """The committed network (trained on the GPU on plain-PatchMatch depth maps of 2000 seeded
-    640x480 scenes) on a held-out scene of the same kind, 4 sweeps. The learned schedule
-    (numOfSamples views from the first sweep, local search) leaves far fewer bad pixels (> 1 %
-    relative depth error) than the plain schedule stopped after 4 sweeps (measured 32.4 % against
-    44.9 %); the same schedule from the random initialisation (threshold 1) does as well or a
-    little better (31.5 %): this network's prediction (about 27 % median depth error, a third of
-    the pixels confident) does not improve on random starting depths, so it must not make them
-    much worse either."""
+    """What the committed network (trained on the GPU on plain-PatchMatch depth maps of 2000
+    seeded 640x480 scenes) gains, on three held-out scenes of the same kind, 4 sweeps each:
+
+    * the learned schedule's gain comes from the schedule: numOfSamples views from the first
+      sweep and the local search leave far fewer bad pixels (> 1 % relative depth error) after
+      4 sweeps than the plain schedule stopped there (about 13 points);
+    * the network adds nothing: at the specified confidence threshold 0.5 its depths cost about
+      a point against the same schedule from random starting depths (threshold 1, the control),
+      and at a threshold of 0.8, where it seeds only its most confident pixels, it is within half
+      a point of the control. Its prediction (about 27 % median depth error) is too coarse to
+      improve on random starts; the test fails if that changes, in either direction."""
     from patchmatch_cuda_gb300 import INIT_PROPOSAL, Engine, proposal, scene
     if not proposal.WEIGHTS.exists():
         pytest.skip("no trained weights in the package")
-    wl = proposal.training_workload(987654)  # seed outside the training range
-    sv = scene.make_views(wl)
+    rows = []
+    for seed in (987654, 987655, 987656):  # seeds outside the training range
+        wl = proposal.training_workload(seed)
+        sv = scene.make_views(wl)
 
-    def bad(**over):
-        e = Engine(sv.images, sv.ref_id, wl.params(**over))
-        net = proposal.for_engine(e) if over.get("init_mode") == INIT_PROPOSAL else None
-        e.run()
-        r = scene.bad_pixel_rate(e.depth(), sv.gt_depth)
-        e.close()
-        if net is not None:
-            net.close()
-        return r
+        def bad(**over):
+            e = Engine(sv.images, sv.ref_id, wl.params(**over))
+            net = proposal.for_engine(e) if over.get("init_mode") == INIT_PROPOSAL else None
+            e.run()
+            r = 100 * scene.bad_pixel_rate(e.depth(), sv.gt_depth)
+            e.close()
+            if net is not None:
+                net.close()
+            return r
 
-    learned4 = bad(init_mode=INIT_PROPOSAL, num_sweeps=4, perturbation=0.05)
-    random4 = bad(num_sweeps=4, perturbation=0.05)
-    # the learned schedule with every pixel from the random initialisation (threshold 1)
-    control4 = bad(init_mode=INIT_PROPOSAL, proposal_threshold=1.0, num_sweeps=4, perturbation=0.05)
-    plain20 = bad()
-    parity_log("trained_proposal_640x480", learned_4_sweeps=learned4, random_4_sweeps=random4,
-               control_4_sweeps=control4, plain_20_sweeps=plain20)
-    assert learned4 < random4 - 0.05, (learned4, random4)
-    assert learned4 < plain20 + 0.06, (learned4, plain20)
-    assert learned4 <= control4 + 0.02, (learned4, control4)
+        sched = dict(init_mode=INIT_PROPOSAL, num_sweeps=4, perturbation=0.05)
+        rows.append({"seed": seed, "learned_0p5": bad(**sched), "learned_0p8": bad(proposal_threshold=0.8, **sched),
+                     "control": bad(proposal_threshold=1.0, **sched), "plain_4": bad(num_sweeps=4),
+                     "plain_20": bad()})
+    mean = {k: float(np.mean([r[k] for r in rows])) for k in rows[0] if k != "seed"}
+    parity_log("trained_proposal_640x480_heldout", scenes=rows, mean_bad_pixel_pct=mean)
+    assert mean["plain_4"] - mean["control"] > 5.0, mean
+    assert -0.5 <= mean["learned_0p5"] - mean["control"] <= 2.0, mean
+    assert abs(mean["learned_0p8"] - mean["control"]) <= 0.5, mean
