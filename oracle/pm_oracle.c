@@ -193,10 +193,14 @@ void pmo_translation_term(const double r_ref[9], const double t_ref[3], const do
 
 /* ------------------------------------------------------------------------------------
  * GaussianBlurCUDA (GaussianBlurCUDA.cu:73-199): separable row then column filter of a
- * float image with zero border. Width = (int)(5*sigma), made odd, clamped to [5, 45]
- * (:99-115). mode 1 ("box") keeps the reference class as written, which overwrites the
- * Gaussian weights with 1/width (:128-129); mode 2 uses the normalised Gaussian weights
- * the class computes before that overwrite; mode 0 copies.
+ * float image. The class reads its input through a texture reference whose modes it never
+ * sets (:22, :132-149), so the defaults hold: point filtering and clamp addressing, a tap
+ * outside the image reads the nearest edge pixel. Width = (int)(5*sigma), made odd, clamped
+ * to [5, 45] (:99-115). mode 1 ("box") keeps the reference class as written, which
+ * overwrites the Gaussian weights with 1/width (:128-129); mode 2 uses the Gaussian weights
+ * the class computes before that overwrite, normalised to sum 1 (the class's normalisation
+ * is commented out, :125-126); mode 0 copies. Taps are summed in the kernels' order,
+ * k = -radius .. radius with weight[radius - k] (:49, :67).
  * ---------------------------------------------------------------------------------- */
 int pmo_prefilter(const float *in, int width, int height, int mode, float sigma, float *out)
 {
@@ -227,8 +231,8 @@ int pmo_prefilter(const float *in, int width, int height, int mode, float sigma,
         for (int x = 0; x < width; ++x) {
             real s = 0;
             for (int k = -radius; k <= radius; ++k) {
-                int xx = x + k;
-                real v = (xx >= 0 && xx < width) ? (real)in[(size_t)y * width + xx] : 0;
+                const int xx = x + k < 0 ? 0 : (x + k >= width ? width - 1 : x + k);
+                const real v = (real)in[(size_t)y * width + xx];
                 s += v * weights[radius - k];
             }
             tmp[(size_t)y * width + x] = s;
@@ -238,8 +242,8 @@ int pmo_prefilter(const float *in, int width, int height, int mode, float sigma,
         for (int x = 0; x < width; ++x) {
             real s = 0;
             for (int k = -radius; k <= radius; ++k) {
-                int yy = y + k;
-                real v = (yy >= 0 && yy < height) ? tmp[(size_t)yy * width + x] : 0;
+                const int yy = y + k < 0 ? 0 : (y + k >= height ? height - 1 : y + k);
+                const real v = tmp[(size_t)yy * width + x];
                 s += v * weights[radius - k];
             }
             out[(size_t)y * width + x] = (float)s;

@@ -13,6 +13,7 @@ baseline where it is available.
                             wide=True: the same code with its floats widened to double.
     ref = RefProblem.from_images(images, ref_id, params, wide=...)
     ref.box_moments(), ref.ncc(...), ref.initial_costs(depth), ref.sweep(...), ref.run(...)
+    blur(img, sigma, wide)  GaussianBlurCUDA::Filter as written (box taps, clamped edges)
 
 Random numbers: the reference's curand states become sequential Philox streams, one per pixel
 state as in array2d_psng (draw k of state id = Philox4x32-10 of counter (id, k, 0x5EED << 16, 0));
@@ -57,9 +58,9 @@ def build() -> None:
 
 
 def extracted_present() -> bool:
-    """The reference's kernels extracted from its sources (ref_kernels.inc) are here: the
+    """The reference's kernels extracted from its sources (ref_kernels.inc, ref_blur.inc) are here: the
     libraries can be built even where the sources are not."""
-    return (REF_OUT / "ref_kernels.inc").exists()
+    return all((REF_OUT / f).exists() for f in ("ref_kernels.inc", "ref_blur.inc"))
 
 
 def available() -> bool:
@@ -88,6 +89,7 @@ def load(wide: bool = False) -> C.CDLL:
     lib.pmr_ncc.argtypes = [P, C.c_int, P, P, P, P, P, P]
     lib.pmr_messages.argtypes = [C.c_int, C.c_int, P, P, C.c_double, C.c_uint64, C.c_uint32, P]
     lib.pmr_find_min_cost.argtypes = [P]
+    lib.pmr_blur.argtypes = [C.c_int, C.c_int, C.c_double, P, P, P]
     _libs[wide] = lib
     return lib
 
@@ -209,3 +211,15 @@ def messages(forward: bool, msg, cost, sp_alpha: float, seed: int, state_id: int
 def find_min_cost(c, wide=False) -> int:
     a = np.ascontiguousarray(c, np.float64)
     return load(wide).pmr_find_min_cost(a.ctypes.data)
+
+
+def blur(img, sigma: float, wide: bool = False):
+    """GaussianBlurCUDA::Filter(dst, src) (GaussianBlurCUDA.cu:185-191) of a float image for an
+    object made with this sigma. Returns (filtered image as float64, the filter width)."""
+    lib = load(wide)
+    a = np.ascontiguousarray(img, np.float64)
+    out = np.empty_like(a)
+    taps = C.c_int(0)
+    if lib.pmr_blur(a.shape[1], a.shape[0], float(sigma), a.ctypes.data, out.ctypes.data, C.byref(taps)) != 0:
+        raise ValueError(f"GaussianBlurCUDA runs no pass for sigma {sigma} (width {taps.value})")
+    return out, taps.value

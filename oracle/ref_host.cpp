@@ -7,7 +7,9 @@
  * ref_extract.sh): sumI_II_RowsKernel / sumI_II_ColsKernel (array2d_refImg.cu:11-67),
  * generate_kernel_float (array2d_wrapper.cu:3-20), computeNCC, findMinCost,
  * readImageIntoSharedMemory, computeMessageBackward / computeMessageForward,
- * computeAllCostGivenDepth, topToDown and downToTop (patchMatch.cu:409-1209). This file
+ * computeAllCostGivenDepth, topToDown and downToTop (patchMatch.cu:409-1209), and
+ * GaussianBlurCUDA's convolutionRowsKernel / convolutionColsKernel / CreateFilterKernel
+ * (GaussianBlurCUDA.cu:39-70, :99-130; ref_blur.inc). This file
  * plays the host side the reference's PatchMatch class plays (patchMatch.cu:51-407): the
  * packed source layers and the homography table as textures (:51-130, :152-205), the
  * reference-window sums (array2d_refImg.cu:70-131), the transposes before and after the
@@ -31,6 +33,7 @@
 #include <barrier>
 #include <chrono>
 #include <thread>
+#include <type_traits>
 #include <vector>
 
 thread_local pmr_dim3 threadIdx, blockIdx;
@@ -71,6 +74,10 @@ static inline double pmr_exp_flushed(double x)
 #define float double
 #endif
 #include "ref_kernels.inc"
+// GaussianBlurCUDA's kernels in a namespace of their own: their texture is named tex32F0 too.
+namespace ref_blur {
+#include "ref_blur.inc"
+}
 #if PMR_WIDE
 #undef float
 #undef exp
@@ -210,6 +217,14 @@ namespace {
 
 using PR = pmr_real;
 
+// The address mode the reference's host code gives each of its textures (patchMatch.cu:192-204,
+// array2d_refImg.cu:109-113): 0 outside the array.
+template <class Tex>
+void set_border(Tex &t)
+{
+    for (auto &m : t.addressMode) m = cudaAddressModeBorder;
+}
+
 // The device-side state of one PatchMatch object (textures, constants, reference maps).
 struct Device {
     const pmr_problem *p;
@@ -225,12 +240,14 @@ struct Device {
         allImgsTexture.width = p->src_width;
         allImgsTexture.height = p->src_height;
         allImgsTexture.layers = p->n_src;
+        set_border(allImgsTexture);
         allImgsTexture.filterMode = cudaFilterModeLinear;
         allImgsTexture.fixed_point_weights = p->fixed_point_weights;
         refImgTexture.data = p->ref;
         refImgTexture.width = p->width;
         refImgTexture.height = p->height;
         refImgTexture.layers = 1;
+        set_border(refImgTexture);
         refImgTexture.filterMode = cudaFilterModeLinear;
         refImgTexture.fixed_point_weights = 0;  // sampled at texel centres: exact either way
         hh.assign(p->hh, p->hh + 18 * (size_t)p->n_src);
@@ -238,6 +255,7 @@ struct Device {
         transformTexture.width = 18;
         transformTexture.height = p->n_src;
         transformTexture.layers = 1;
+        set_border(transformTexture);
         transformTexture.filterMode = cudaFilterModePoint;
         orientation[0] = (PR)p->orientation[0];
         orientation[1] = (PR)p->orientation[1];
@@ -262,6 +280,7 @@ struct Device {
         tex32F0.width = w;
         tex32F0.height = h;
         tex32F0.layers = 1;
+        set_border(tex32F0);  // array2d_refImg.cu:109-110
         tex32F0.filterMode = cudaFilterModeLinear;
         launch_2d(w, h, 16, 12, [&] {
             sumI_II_RowsKernel<FR>(ref_i.ptr(), sum_i.ptr(), sum_ii.ptr(), w, h, sum_i.pitch());
@@ -272,6 +291,7 @@ struct Device {
             tex32F0_float.width = w;
             tex32F0_float.height = h;
             tex32F0_float.layers = 1;
+            set_border(tex32F0_float);  // array2d_refImg.cu:112-113
             tex32F0_float.filterMode = cudaFilterModeLinear;
             launch_2d(w, h, 16, 12, [&] { sumI_II_ColsKernel<FR>(m->ptr(), w, h, m->pitch()); });
         }
@@ -585,6 +605,47 @@ int pmr_find_min_cost(const double cost[3])
 {
     PR c[3] = {(PR)cost[0], (PR)cost[1], (PR)cost[2]};
     return findMinCost(c);
+}
+
+// GaussianBlurCUDA::Filter(float *dst, const float *src) (GaussianBlurCUDA.cu:185-191) of an
+// object made for (width, height, sigma) (:73-89): CreateFilterKernel (:99-130) fills g_Kernel,
+// Filter switches on the radius (:152-183) and FilterImage<FR> (:132-149) runs the row pass
+// over the source bound to tex32F0, then the column pass over the row pass's output, in blocks
+// of 16 x 12 threads (:13-14, :134-135). The texture keeps the defaults of its declaration
+// (:22; the class sets no mode): point filtering, clamp addressing. Writes the taps' count to
+// *taps (the filter width); returns -1 where Filter runs no pass (a radius outside 2..22).
+int pmr_blur(int width, int height, double sigma, const double *src, double *dst, int *taps)
+{
+    namespace B = ref_blur;
+    auto &tex = B::tex32F0;
+    PR filter_kernel[KERNEL_MAX_WIDTH];  // float as written, double in the widened build
+    int kw = 0;
+    B::GaussianBlurCUDA_CreateFilterKernel((PR)sigma, filter_kernel, kw);
+    *taps = kw;
+    for (int i = 0; i < kw; ++i) B::g_Kernel[i] = filter_kernel[i];
+    const size_t n = (size_t)width * height;
+    std::vector<PR> in(src, src + n), tmp(n), out(n);
+    tex.width = width;
+    tex.height = height;
+    tex.layers = 1;
+    auto filter = [&](auto fr) {
+        constexpr int FR = decltype(fr)::value;
+        tex.data = in.data();
+        launch_2d(width, height, THREADS_NUMBER_H, THREADS_NUMBER_V,
+                  [&] { B::convolutionRowsKernel<FR>(tmp.data(), width, height); });
+        tex.data = tmp.data();
+        launch_2d(width, height, THREADS_NUMBER_H, THREADS_NUMBER_V,
+                  [&] { B::convolutionColsKernel<FR>(out.data(), width, height); });
+    };
+    switch (kw >> 1) {
+#define X(n) case n: filter(std::integral_constant<int, n>{}); break;
+        X(2) X(3) X(4) X(5) X(6) X(7) X(8) X(9) X(10) X(11) X(12)
+        X(13) X(14) X(15) X(16) X(17) X(18) X(19) X(20) X(21) X(22)
+#undef X
+    default: return -1;
+    }
+    for (size_t i = 0; i < n; ++i) dst[i] = (double)out[i];
+    return 0;
 }
 
 }  // extern "C"

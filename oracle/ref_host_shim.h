@@ -9,8 +9,11 @@
  *    shared arrays are shared by the threads of the block that runs (blocks run one after
  *    another; ref_host.cpp runs a block's 32 threads as 32 host threads).
  *  - threadIdx / blockIdx are per host thread; blockDim is the launch's.
- *  - texture<T, cudaTextureType2DLayered, mode> references and tex2DLayered: a layered array
- *    of texels with border addressing (0 outside), point or linear filtering in CUDA's
+ *  - texture<T, type, mode> references with CUDA's defaults for a texture reference (clamp
+ *    addressing, point filtering, unnormalised coordinates): the host code sets the modes the
+ *    reference's host code sets. tex2DLayered reads a layered array of texels, tex2D a 2-D one
+ *    (layer 0). Border addressing reads 0 outside the array, clamp addressing the nearest edge
+ *    texel. Point or linear filtering in CUDA's
  *    documented convention (texel i centred at coordinate i + 0.5; linear filtering weights
  *    the 2x2 texels around (x - 0.5, y - 0.5) by their fractions), uchar texels read as the
  *    float value / 255 (cudaReadModeNormalizedFloat). Linear weights are either exact or the
@@ -55,17 +58,17 @@ struct pmr_dim3 {
 extern thread_local pmr_dim3 threadIdx, blockIdx;
 extern pmr_dim3 blockDim, gridDim;
 
-enum pmr_texture_type { cudaTextureType2DLayered = 0xF2 };
+enum pmr_texture_type { cudaTextureType2D = 0x02, cudaTextureType2DLayered = 0xF2 };
 enum cudaTextureReadMode { cudaReadModeElementType = 0, cudaReadModeNormalizedFloat = 1 };
 enum cudaTextureAddressMode { cudaAddressModeWrap, cudaAddressModeClamp, cudaAddressModeMirror, cudaAddressModeBorder };
 enum cudaTextureFilterMode { cudaFilterModePoint, cudaFilterModeLinear };
 
-/* A texture reference bound to a layered array of width x height texels per layer. */
+/* A texture reference bound to a (layered) array of width x height texels per layer. */
 template <class T, int type, cudaTextureReadMode mode>
 struct texture {
     const T *data = nullptr;
     int width = 0, height = 0, layers = 0;
-    cudaTextureAddressMode addressMode[3] = {cudaAddressModeBorder, cudaAddressModeBorder, cudaAddressModeBorder};
+    cudaTextureAddressMode addressMode[3] = {cudaAddressModeClamp, cudaAddressModeClamp, cudaAddressModeClamp};
     cudaTextureFilterMode filterMode = cudaFilterModePoint;
     int normalized = 0;
     int fixed_point_weights = 0;                 /* linear filtering: 1/256 weights */
@@ -74,6 +77,8 @@ struct texture {
 template <class T, int type, cudaTextureReadMode mode>
 static inline pmr_real pmr_texel(const texture<T, type, mode> &t, int x, int y, int layer)
 {
+    if (t.addressMode[0] == cudaAddressModeClamp) x = x < 0 ? 0 : (x >= t.width ? t.width - 1 : x);
+    if (t.addressMode[1] == cudaAddressModeClamp) y = y < 0 ? 0 : (y >= t.height ? t.height - 1 : y);
     if (x < 0 || y < 0 || x >= t.width || y >= t.height) return (pmr_real)0;
     const T v = t.data[((size_t)layer * t.height + y) * t.width + x];
     /* the texture unit returns a normalized texel as the float v / 255 */
@@ -99,9 +104,13 @@ static pmr_real tex2DLayered(const texture<T, type, mode> &t, pmr_real x, pmr_re
     if (t.filterMode == cudaFilterModePoint) {
         const double fx = floor((double)x), fy = floor((double)y);
         if (fy < 0.0 || fy >= (double)t.height) ++pmr_point_outside;
-        if (fx < 0.0 || fy < 0.0 || fx >= (double)t.width || fy >= (double)t.height) return (pmr_real)0;
-        return pmr_texel(t, (int)fx, (int)fy, layer);
+        if (t.addressMode[0] != cudaAddressModeClamp && (fx < 0.0 || fx >= (double)t.width)) return (pmr_real)0;
+        if (t.addressMode[1] != cudaAddressModeClamp && (fy < 0.0 || fy >= (double)t.height)) return (pmr_real)0;
+        const double cx = fx < 0.0 ? -1.0 : (fx > (double)t.width ? (double)t.width : fx);
+        const double cy = fy < 0.0 ? -1.0 : (fy > (double)t.height ? (double)t.height : fy);
+        return pmr_texel(t, (int)cx, (int)cy, layer);
     }
+    /* linear filtering: border addressing, the reference's only linear textures */
     const pmr_real xb = x - (pmr_real)0.5, yb = y - (pmr_real)0.5;
     if (!(xb > (pmr_real)-1 && xb < (pmr_real)t.width && yb > (pmr_real)-1 && yb < (pmr_real)t.height))
         return (pmr_real)0;
@@ -118,6 +127,21 @@ static pmr_real tex2DLayered(const texture<T, type, mode> &t, pmr_real x, pmr_re
     }
     return ((pmr_real)1 - a) * ((pmr_real)1 - b) * t00 + a * ((pmr_real)1 - b) * t10 +
            ((pmr_real)1 - a) * b * t01 + a * b * t11;
+}
+
+/* A non-layered 2-D texture reference (GaussianBlurCUDA.cu:22): layer 0 of the bound array. */
+template <class T, cudaTextureReadMode mode>
+static inline pmr_real tex2D(const texture<T, cudaTextureType2D, mode> &t, pmr_real x, pmr_real y)
+{
+    return tex2DLayered(t, x, y, 0);
+}
+
+/* __mul24: the product of the low 24 bits of a and b, each read as a signed 24-bit integer;
+ * the low 32 bits of the 48-bit product. */
+static inline int __mul24(int a, int b)
+{
+    const int64_t a24 = (int64_t)(int32_t)((uint32_t)a << 8) >> 8, b24 = (int64_t)(int32_t)((uint32_t)b << 8) >> 8;
+    return (int)(uint32_t)(uint64_t)(a24 * b24);
 }
 
 /* ---- random numbers ------------------------------------------------------------------------ */

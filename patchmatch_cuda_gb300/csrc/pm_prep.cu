@@ -25,8 +25,10 @@ __global__ void u8_to_float_kernel(const uint8_t *__restrict__ in, int in_pitch,
     if (x < w && y < h) out[(size_t)y * w + x] = (float)in[(size_t)y * in_pitch + x] / 255.0f;
 }
 
-// One 1-D pass of the separable filter with zero border; dir 0 = along x, 1 = along y.
-// Taps are applied in the reference's order (k = -radius .. radius, weight[radius - k]).
+// One 1-D pass of the separable filter; dir 0 = along x, 1 = along y. A tap outside the image
+// reads the nearest edge pixel: the reference class samples a texture reference left at its
+// default clamp addressing (GaussianBlurCUDA.cu:22). Taps are applied in the reference's order
+// (k = -radius .. radius, weight[radius - k]).
 __global__ void filter_pass_kernel(const float *__restrict__ in, float *__restrict__ out, int w,
                                    int h, int radius, int dir, const FilterTaps taps)
 {
@@ -34,9 +36,9 @@ __global__ void filter_pass_kernel(const float *__restrict__ in, float *__restri
     if (x >= w || y >= h) return;
     float s = 0.0f;
     for (int k = -radius; k <= radius; ++k) {
-        const int xx = dir == 0 ? x + k : x, yy = dir == 0 ? y : y + k;
-        const float v = (xx >= 0 && xx < w && yy >= 0 && yy < h) ? in[(size_t)yy * w + xx] : 0.0f;
-        s += v * taps.w[radius - k];
+        const int xx = dir == 0 ? min(max(x + k, 0), w - 1) : x;
+        const int yy = dir == 0 ? y : min(max(y + k, 0), h - 1);
+        s += in[(size_t)yy * w + xx] * taps.w[radius - k];
     }
     out[(size_t)y * w + x] = s;
 }

@@ -1,9 +1,11 @@
 """Writes tests/golden/ref_box200_96x64.npz: outputs of the REFERENCE'S OWN KERNELS
-(yhsa678/patchMatch_cuda's patchMatch.cu, array2d_refImg.cu and array2d_wrapper.cu, run on the
-CPU by oracle/ref_host.cpp) on a 96x64 crop of the benchmarked scene (box200_1280x720: 12 planes
-+ 200 boxes) with its window, view count and sample count (15x15, 10 sources, numOfSamples 5,
-depth [1, 20], no prefilter); each source is cut to where the crop can project (crop_views). The oracle (pm_oracle.c) must reproduce them; the engine is checked against them on
-the GPU. Two builds of the reference write them: "f32" computes as the reference is written,
+(yhsa678/patchMatch_cuda's patchMatch.cu, array2d_refImg.cu, array2d_wrapper.cu and
+GaussianBlurCUDA.cu, run on the CPU by oracle/ref_host.cpp) on a 96x64 crop of the benchmarked
+scene (box200_1280x720: 12 planes + 200 boxes) with its window, view count and sample count
+(15x15, 10 sources, numOfSamples 5, depth [1, 20], no prefilter); each source is cut to where
+the crop can project (crop_views). The oracle (pm_oracle.c) must reproduce them
+(tests/test_ref_pin.py); the engine is checked against the parts that draw no random numbers on
+the GPU (tests/test_gpu_refpin.py). Two builds of the reference write them: "f32" computes as the reference is written,
 "f64" is the same code with its floats widened to double (the reference's rules without float
 rounding, which the FP64 oracle must agree with to rounding level).
 
@@ -27,6 +29,8 @@ Contents (arrays of the f64 build are stored in float64 unless named otherwise):
   msg_*                                      computeMessageForward/Backward cases
   min_cost_in, min_cost_idx                  findMinCost on ties and orderings
   run_depth_*, run_view_sel_*                a 3-iteration run (random states in stream order)
+  blur{i}_*, blur_sigma, blur_taps           GaussianBlurCUDA::Filter of the reference image
+                                             (u8 / 255) for each sigma, and its filter width
 """
 import sys
 from pathlib import Path
@@ -48,6 +52,8 @@ CROP_DEPTHS = (2.2, 9.0)
 CROP_MARGIN = 16
 WORKLOAD = scene.Workload("ref_box200_96x64", 96, 64, 10, 7, 3, 1.0, 20.0, 12, 200, prefilter=0, seed=2024)
 BAND = 16
+# GaussianBlurCUDA objects: the smallest width (5 taps), a middle one and the largest (45)
+BLUR_SIGMAS = (1.0, 2.0, 9.5)
 
 
 def params(w=WORKLOAD):
@@ -197,6 +203,13 @@ def compute(sv, wide: bool, start=None) -> dict:
     out[f"run_depth_{tag}"] = depth.astype(np.float32)
     out[f"run_view_sel_{tag}"] = vsel
     out[f"run_outside_{tag}"] = np.int64(outside)
+    img = sv.images[sv.ref_id].image.astype(np.float32) / np.float32(255)
+    taps = []
+    for i, sigma in enumerate(BLUR_SIGMAS):
+        b, kw = pm_ref.blur(img, sigma, wide=wide)
+        out[f"blur{i}_{tag}"] = b.astype(ft)
+        taps.append(kw)
+    out["blur_sigma"], out["blur_taps"] = np.array(BLUR_SIGMAS), np.array(taps, np.int32)
     return out
 
 

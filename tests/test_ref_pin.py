@@ -2,8 +2,9 @@
 
 tests/golden/ref_box200_96x64.npz holds outputs of yhsa678/patchMatch_cuda's own kernels --
 patchMatch.cu's computeNCC, computeMessageForward/Backward, findMinCost,
-computeAllCostGivenDepth, topToDown and downToTop, array2d_refImg.cu's window sums and
-array2d_wrapper.cu's random initial depth -- compiled for the CPU and run by oracle/ref_host.cpp
+computeAllCostGivenDepth, topToDown and downToTop, array2d_refImg.cu's window sums,
+array2d_wrapper.cu's random initial depth and GaussianBlurCUDA.cu's filter -- compiled for the
+CPU and run by oracle/ref_host.cpp
 (make_ref_golden.py wrote it), on a 96x64 crop of the benchmarked scene with its window, view
 and sample counts (15x15, 10 sources, numOfSamples 5). Two builds of the reference wrote it:
 "f32" computes as the reference is written (float, flush-to-zero as under --use_fast_math);
@@ -207,6 +208,26 @@ def test_find_min_cost_matches_reference(golden, oracle_lib):
     np.testing.assert_array_equal(got, golden["min_cost_idx_f32"])
 
 
+def test_prefilter_matches_reference_blur(golden, oracle_lib):
+    """GaussianBlurCUDA::Filter (GaussianBlurCUDA.cu:185-191) as written, the oracle's box
+    prefilter: taps of 1/width, width (int)(5 sigma) made odd within [5, 45], edge pixels
+    repeated outside the image (the class's texture keeps its default clamp addressing). The
+    oracle's FP32 build reproduces the reference's float build bit for bit; the FP64 oracle,
+    whose output is float, the widened build within that rounding."""
+    from oracle import pm_oracle
+    img = golden[f"image_{int(golden['ref_id'])}"].astype(np.float32) / np.float32(255)
+    np.testing.assert_array_equal(golden["blur_taps"], [5, 11, 45])
+    for i, sigma in enumerate(golden["blur_sigma"]):
+        np.testing.assert_array_equal(pm_oracle.prefilter(img, 1, float(sigma), fp32=True), golden[f"blur{i}_f32"])
+        assert np.abs(pm_oracle.prefilter(img, 1, float(sigma)) - golden[f"blur{i}_f64"]).max() <= 6e-8
+        # the same filter over the image padded with its edge pixels
+        kw = int(golden["blur_taps"][i])
+        pad = np.pad(img.astype(np.float64), kw // 2, mode="edge")
+        rows = np.stack([pad[:, k:k + img.shape[1]] for k in range(kw)]).sum(0) / kw
+        box = np.stack([rows[k:k + img.shape[0]] for k in range(kw)]).sum(0) / kw
+        assert np.abs(box - golden[f"blur{i}_f64"]).max() <= 1e-12
+
+
 def test_full_run_matches_reference(orc, golden, parity_log):
     """PatchMatch::run<15> (patchMatch.cu:307-394), 3 iterations from the random initial depth,
     random states drawn in the reference's order: the final depths of the reference as written
@@ -284,3 +305,20 @@ def test_whole_run_lockstep_against_reference(golden, orc, wide, parity_log):
         orc.set_stream(None)
     parity_log(f"ref_pin_whole_run_lockstep_{'f64' if wide else 'f32'}", divergences=events, decisions=decisions)
     assert events <= (0 if wide else 2e-4 * decisions), f"{events} divergences in {decisions} decisions"
+
+
+@needs_reference
+@pytest.mark.parametrize("shape", [(1, 1), (5, 7), (64, 3), (37, 53)])
+def test_blur_against_reference(shape, oracle_lib):
+    """The reference's blur on images smaller than its filter and on ragged shapes, for widths
+    at and beyond both clamps (sigma 0.1 -> 5 taps, 1.4 -> 7, 20 -> 45): the oracle's FP32
+    build equal bit for bit, its filter width the reference's."""
+    from oracle import pm_oracle, pm_ref
+    rng = np.random.default_rng(sum(shape))
+    img = rng.integers(0, 256, shape).astype(np.float32) / np.float32(255)
+    for sigma, taps in [(0.1, 5), (1.0, 5), (1.4, 7), (3.0, 15), (20.0, 45)]:
+        r32, kw = pm_ref.blur(img, sigma)
+        r64, kw64 = pm_ref.blur(img, sigma, wide=True)
+        assert kw == kw64 == taps
+        np.testing.assert_array_equal(pm_oracle.prefilter(img, 1, sigma, fp32=True), r32.astype(np.float32))
+        assert np.abs(pm_oracle.prefilter(img, 1, sigma) - r64).max() <= 6e-8
