@@ -3,6 +3,13 @@ of one sweep (first divergence per line, the mask of matched steps, view-selecti
 import numpy as np
 
 NCC_TOL = 1e-4
+# The exact sampler's tail. It forms source coordinates and bilinear fractions in FP32, the
+# oracle in FP64; near a source edge of a prefiltered image (flat to the last texel, whose
+# edge pixels the prefilter repeats, then a step to the zero border within one pixel) the
+# coordinate's float rounding (3e-5 px near x = 300) times that gradient is the NCC's largest
+# error, and a low-variance window there magnifies it. The 99.9th percentile stays within
+# NCC_TOL; those rare windows within EXACT_TAIL_TOL.
+EXACT_TAIL_TOL = 5 * NCC_TOL
 
 
 def ncc_err(got, want):

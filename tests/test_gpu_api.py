@@ -40,7 +40,11 @@ def test_depth_outputs_file_format_and_view_selection(small, tmp_path):
     assert np.all(vs[:, -1, :] == 255)              # the final sweep's first processed row
     body = vs[:, :-1, :]
     assert np.all((body < w.n_src) | (body == 255))
-    assert np.mean(body == 255) < 0.01               # 255: no view (every posterior underflowed)
+    # 255: no view (every emission of the step underflowed, a NaN posterior). That happens only
+    # at the final bottom-to-top sweep's leading edge, the top half-window rows whose cut
+    # windows give costs beyond ~6
+    assert not np.any(body[:, w.half_window + 1:, :] == 255)
+    assert np.mean(body == 255) < 0.02
     st = eng.stats()
     assert st.cost_evals >= st.cost_evals_done > 0 and st.ms_total > 0
     eng.close()

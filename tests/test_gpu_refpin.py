@@ -97,7 +97,8 @@ def test_box_prefilter_matches_reference_blur(golden, parity_log):
     """The engine's box prefilter of the reference image is GaussianBlurCUDA as written: 1/width
     taps, edge pixels repeated. The engine fuses each tap's multiply-add (as nvcc does for the
     reference's `sum += tex2D(..) * g_Kernel[..]`), the host-compiled float build does not: the
-    two differ by float rounding."""
+    two differ by float rounding, at most half an ulp of 1 (values lie in [0, 1]) per add of
+    each pass's taps."""
     errs = []
     for i, sigma in enumerate(golden["blur_sigma"]):
         eng = make_engine(golden, prefilter=1, gaussian_sigma=float(sigma))
@@ -105,7 +106,8 @@ def test_box_prefilter_matches_reference_blur(golden, parity_log):
         e32 = np.abs(ref.astype(np.float64) - golden[f"blur{i}_f32"])
         e64 = np.abs(ref.astype(np.float64) - golden[f"blur{i}_f64"])
         errs.append((float(e32.max()), float(e64.max())))
-        assert e32.max() <= 5e-7 and e64.max() <= 5e-7, (sigma, e32.max(), e64.max())
+        bound = 2 * int(golden["blur_taps"][i]) * 2.0 ** -24
+        assert e32.max() <= bound and e64.max() <= bound, (sigma, e32.max(), e64.max(), bound)
         eng.close()
     parity_log("refpin_gpu_box_prefilter", taps=[int(t) for t in golden["blur_taps"]],
                err_max_vs_float_build=[e[0] for e in errs], err_max_vs_widened=[e[1] for e in errs])
