@@ -386,6 +386,76 @@ __device__ __forceinline__ void ring_window(const RefDesc &D, int x, int y, bool
     if (lane == 0) window_scalars(D, x, y, x0, y0, y0, y0 + W - 1, n, c1, 0.0f, true, wc);
 }
 
+// ring_window for the lines within a half-window of an image edge: windows whose extent along
+// the sweep lies inside the image but which the border cuts across the line, the same cut for
+// every step of the line. The ring holds load_window's values: zeros off the image and, on a
+// line at the leading edge with the reference's misaligned tile (quirks), the shifted values it
+// pairs with the window in `raw` and the unshifted ones in `raw_o`. The table, column sums and
+// leading-edge term are formed with load_window's arithmetic in its order, so both give the
+// same values.
+template <int W>
+__device__ __forceinline__ void ring_window_cut(const RefDesc &D, int x, int y, bool rows, int enter, int lane,
+                                                float *raw, float *raw_o, float *tab, float *col, WinCtl &wc)
+{
+    constexpr int HW = Window<W>::HW;
+    const int Wd = D.width, Hd = D.height;
+    const int x0 = x - HW, y0 = y - HW;
+    const int lead = !D.quirks ? 0 : rows ? (x0 < 0 ? -x0 : 0) : (y0 < 0 ? -y0 : 0);
+    const bool shifted = lead != 0;
+    const int a0 = rows ? x0 : y0, alen = rows ? Wd : Hd;
+    const int cx0 = max(x0, 0), cx1 = min(x + HW, Wd - 1);
+    const int cy0 = max(y0, 0), cy1 = min(y + HW, Hd - 1);
+    const size_t pix = (size_t)y * Wd + x;
+    const float sum_i = __ldg(D.sum_i + pix);
+    const float c1 = lane == 0 ? __ldg(D.c1 + pix) : 0.0f;
+    // the entering line, or every line of the window: lane i is the window's column (rows) or
+    // row (columns) i across the sweep
+    const size_t stride = rows ? 1 : (size_t)Wd;
+#pragma unroll
+    for (int q = 0; q < (W + 31) / 32; ++q) {
+        const int i = lane + 32 * q;
+        if (i >= W) continue;
+        const int ai = a0 + i;                   // image column (rows) or row (columns)
+        const bool in = (unsigned)ai < (unsigned)alen;
+        const bool p_in = in && ai - lead >= 0;  // the shifted read stays on the image
+        const int k0 = enter < 0 ? 0 : W - 1, k1 = W;
+#pragma unroll 1
+        for (int k = k0; k < k1; ++k) {
+            const int along = enter < 0 ? (rows ? y0 : x0) + k : enter;
+            const int slot = rows ? (along % W) * W + i : i * W + along % W;
+            const size_t at = rows ? (size_t)along * Wd : (size_t)along;
+            raw[slot] = p_in ? __ldg(D.ref + at + (size_t)(ai - lead) * stride) : 0.0f;
+            if (shifted) raw_o[slot] = in ? __ldg(D.ref + at + (size_t)ai * stride) : 0.0f;
+        }
+    }
+    __syncwarp();
+    const float n = (float)((cx1 - cx0 + 1) * (cy1 - cy0 + 1));
+    const float mu = sum_i / n;
+    float sh = 0.0f;
+#pragma unroll
+    for (int q = 0; q < (W + 31) / 32; ++q) {
+        const int c = lane + 32 * q;
+        if (c >= W) continue;
+        const bool col_in = !rows || (unsigned)(x0 + c) < (unsigned)Wd;
+        const int cslot = rows ? 0 : (x0 + c) % W;
+        int rslot = rows ? y0 % W : 0;
+        float cs = 0.0f;
+        for (int dy = 0; dy < W; ++dy) {
+            const int at = rows ? rslot * W + c : dy * W + cslot;
+            const bool in = col_in && (rows || (unsigned)(y0 + dy) < (unsigned)Hd);
+            const float v = raw[at];
+            const float b = in ? v - mu : 0.0f;
+            if (in && shifted) sh += v - raw_o[at];
+            rslot = rslot + 1 == W ? 0 : rslot + 1;
+            tab[dy * W + c] = b;
+            cs += b;
+        }
+        col[c] = cs;
+    }
+    if (shifted) sh = warp_sum(sh);
+    if (lane == 0) window_scalars(D, x, y, x0, y0, cy0, cy1, n, c1, shifted ? sh : 0.0f, false, wc);
+}
+
 // A homography's first two columns and its value at the window origin (see warp_setup).
 struct WarpSetup {
     float c0x, c0y, c0z, c1x, c1y, c1z, bx, by, bz;
@@ -625,9 +695,10 @@ __device__ __forceinline__ void ncc_pair_core(const RefDesc &D, const float4 *hh
     }
 }
 
-// Windows cut by the image border: out of line, so the hot loop stays small.
+// Windows cut by the image border. Inline: the lines along the image's edges cut every window,
+// and the sweep lasts as long as its slowest line (an out-of-line call measured 4 % slower).
 template <int W, bool HW, bool PL>
-__device__ __noinline__ void ncc_pair_edge(const RefDesc &D, const float4 *hh, const WinCtl &wc,
+__device__ __forceinline__ void ncc_pair_edge(const RefDesc &D, const float4 *hh, const WinCtl &wc,
                                            const float *tab, const float *col, int lane, int va,
                                            float da, float2 sa, int vb, float db, float2 sb, float &ra,
                                            float &rb)

@@ -169,7 +169,8 @@ __global__ void __maxnreg__(SweepRegs<HW>::value) sweep_kernel(const __grid_cons
     __shared__ float s_res_f[MAX_VIEWS];  // NCC(view, previous step's depth)
     __shared__ float s_res_r[MAX_VIEWS];  // NCC(view, random depth)
     __shared__ float s_new[MAX_VIEWS];    // refreshed costs
-    __shared__ float s_raw[W * W];        // reference values of the current interior window
+    __shared__ float s_raw[W * W];        // reference values of the current window (ring)
+    __shared__ float s_raw_o[W * W];      // the unshifted ones on a leading-edge line (quirks)
     __shared__ float2 s_wsl[2];           // slanted planes: the current slopes of steps k, k+1
     __shared__ float2 s_dsl[3];           // slanted planes: random-slope draws of steps k .. k+2
     __shared__ PlaneCtl s_pctl[2];        // slanted planes: the hypotheses' slopes
@@ -181,15 +182,23 @@ __global__ void __maxnreg__(SweepRegs<HW>::value) sweep_kernel(const __grid_cons
         y = rot ? line : c_;                                 \
     } while (0)
 
-    // step kk's window (loader warp): inside the image from the ring s_raw, sliding it by the
-    // entering line when it holds the previous step's window, otherwise loaded whole
+    // step kk's window (loader warp): when its extent along the sweep lies inside the image,
+    // from the ring s_raw, sliding it by the entering line when it holds the previous step's
+    // window (lines within a half-window of an edge, whose windows the border cuts across the
+    // line, have a variant of their own); otherwise (a line's first and last half-window of
+    // steps) loaded whole
     constexpr int HWIN = Window<W>::HW;
+    const bool cut_line = line < HWIN || line + HWIN >= (rot ? Hd : Wd);
     int ring_step = -1;  // the step whose window the ring holds
     auto load_step = [&](int kk, int xn, int yn) {
-        if (xn >= HWIN && yn >= HWIN && xn + HWIN < Wd && yn + HWIN < Hd) {
+        if (rot ? (xn >= HWIN && xn + HWIN < Wd) : (yn >= HWIN && yn + HWIN < Hd)) {
             const int enter = ring_step != kk - 1 ? -1
                               : rot ? (fwd ? xn + HWIN : xn - HWIN) : (fwd ? yn + HWIN : yn - HWIN);
-            ring_window<W>(D, xn, yn, !rot, enter, lane, s_raw, s_tab[kk & 1], s_col[kk & 1], s_win[kk & 1]);
+            if (cut_line)
+                ring_window_cut<W>(D, xn, yn, !rot, enter, lane, s_raw, s_raw_o, s_tab[kk & 1], s_col[kk & 1],
+                                   s_win[kk & 1]);
+            else
+                ring_window<W>(D, xn, yn, !rot, enter, lane, s_raw, s_tab[kk & 1], s_col[kk & 1], s_win[kk & 1]);
             ring_step = kk;
         } else {
             load_window<W>(D, xn, yn, axis, lane, s_tab[kk & 1], s_col[kk & 1], s_win[kk & 1]);
@@ -218,19 +227,33 @@ __global__ void __maxnreg__(SweepRegs<HW>::value) sweep_kernel(const __grid_cons
     // the NCC passes; a step's current slopes, loaded with its window (s_wsl[k & 1])
     __shared__ float4 s_former;
     unsigned long long n_alg = 0, n_done = 0;
+    // backward messages in reverse processing order (patchMatch.cu:856-869, :1050-1059). Every
+    // step's emissions are independent of the messages: all warps form them first (with the
+    // cost-2 replacement draws) into the line's message buffer, then warp 0 runs the recurrence
+    // over them, loading PB steps at a time so that their latency overlaps
+    for (int i = threadIdx.x; i < nsteps * V; i += blockDim.x) {
+        const int k = i / V, v = i - k * V;
+        int x, y;
+        PM_PIXEL(k, x, y);
+        const uint32_t pix = (uint32_t)(y * Wd + x);
+        float c = cost[(size_t)pix * V + v];
+        if (c == 2.0f) c = 2.0f * draw_uniform(D.seed, pix, sweep, RNG_BWD, v, D.batch_id);
+        bline[i] = emission(c, a2);
+    }
+    __syncthreads();
     if (warp == 0) {
-        // backward messages in reverse processing order (patchMatch.cu:856-869, :1050-1059)
         float beta = 0.5f;
-#pragma unroll 4
-        for (int k = nsteps - 1; k >= 0; --k) {
-            int x, y;
-            PM_PIXEL(k, x, y);
-            const uint32_t pix = (uint32_t)(y * Wd + x);
-            if (vl) {
-                bline[(size_t)k * V + lane] = beta;
-                float c = cost[(size_t)pix * V + lane];
-                if (c == 2.0f) c = 2.0f * draw_uniform(D.seed, pix, sweep, RNG_BWD, lane, D.batch_id);
-                beta = msg_backward(beta, emission(c, a2), u_emit);
+        constexpr int PB = 16;
+        for (int k0 = nsteps - 1; k0 >= 0; k0 -= PB) {
+            float e[PB];
+#pragma unroll
+            for (int j = 0; j < PB; ++j) e[j] = vl && k0 - j >= 0 ? bline[(size_t)(k0 - j) * V + lane] : 0.0f;
+#pragma unroll
+            for (int j = 0; j < PB; ++j) {
+                if (vl && k0 - j >= 0) {
+                    bline[(size_t)(k0 - j) * V + lane] = beta;
+                    beta = msg_backward(beta, e[j], u_emit);
+                }
             }
         }
         // forward message at the first step (patchMatch.cu:872-874)
