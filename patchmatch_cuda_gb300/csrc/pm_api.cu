@@ -23,6 +23,9 @@ struct pm_handle {
     int device = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    // a sweep's edge lines run on `side`, forked from and joined back to `stream`
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
     pm_params p{};
     int W = 0, H = 0, V = 0, win = 0;
     int texel_bytes = 4;
@@ -45,6 +48,7 @@ struct pm_handle {
     SweepArgs *h_sweep_args = nullptr;   // pinned, one per sweep of the schedule
 
     int wpl[2] = {0, 0};                // warps per line: [vertical sweeps, horizontal sweeps]
+    int wpl_edge[2] = {0, 0};           // the same for the launch of the lines along the edges
     // learned proposal
     pm_net *net = nullptr;
     ProposalGeom geom{};
@@ -287,9 +291,21 @@ void fill_sweep_args(SweepArgs &a, const RefDesc *refs, const int *lines, int nr
     a.record_views = record;
     a.perturb = 0.0f;
     a.decay = std::exp2(-0.25f * (float)sweep_id);
+    a.line_mode = LINES_ALL;
     a.line_start[0] = 0;
     for (int i = 0; i < nrefs; ++i) a.line_start[i + 1] = a.line_start[i] + lines[i];
     a.total_lines = a.line_start[nrefs];
+}
+
+// The same sweep restricted to the lines of `mode` (lines: each reference's lines of the sweep).
+SweepArgs sweep_args_mode(const SweepArgs &all, const int *lines, int win, int mode)
+{
+    SweepArgs a = all;
+    a.line_mode = mode;
+    a.line_start[0] = 0;
+    for (int i = 0; i < a.nrefs; ++i) a.line_start[i + 1] = a.line_start[i] + mode_lines(mode, lines[i], win / 2);
+    a.total_lines = a.line_start[a.nrefs];
+    return a;
 }
 
 cudaError_t enqueue_sweep(int win, bool hw, bool pl, int wpl, const SweepArgs &a, cudaStream_t s)
@@ -302,6 +318,25 @@ cudaError_t enqueue_sweep(int win, bool hw, bool pl, int wpl, const SweepArgs &a
     req.grid = a.total_lines;
     req.block = 32 * wpl;
     return launch_window(win, hw, pl, req);
+}
+
+// One sweep of every line (`all`, LINES_ALL), as two concurrent launches when it has both
+// interior and edge lines: the interior lines on s with wpl warps per line, the edge lines on
+// `side` with wpl_edge, forked from s and joined back to it (graph edges under stream capture).
+cudaError_t enqueue_sweep_split(int win, bool hw, bool pl, int wpl, int wpl_edge, const SweepArgs &all,
+                                const int *lines, cudaStream_t s, cudaStream_t side, cudaEvent_t fork,
+                                cudaEvent_t join)
+{
+    const SweepArgs ai = sweep_args_mode(all, lines, win, LINES_INTERIOR);
+    const SweepArgs ae = sweep_args_mode(all, lines, win, LINES_EDGES);
+    if (!side || ai.total_lines == 0 || ae.total_lines == 0) return enqueue_sweep(win, hw, pl, wpl, all, s);
+    cudaError_t e = cudaEventRecord(fork, s);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(side, fork, 0);
+    if (e == cudaSuccess) e = enqueue_sweep(win, hw, pl, wpl_edge, ae, side);
+    if (e == cudaSuccess) e = cudaEventRecord(join, side);
+    if (e == cudaSuccess) e = enqueue_sweep(win, hw, pl, wpl, ai, s);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, join, 0);
+    return e;
 }
 
 
@@ -337,6 +372,14 @@ void tuned_store(const TuneKey &k, int wpl)
 int lines_of(const pm_handle *h, int dir)
 {
     return (dir == PM_DIR_LEFT_TO_RIGHT || dir == PM_DIR_RIGHT_TO_LEFT) ? h->H : h->W;
+}
+
+// A sweep of the handle's reference: interior and edge lines as two concurrent launches.
+cudaError_t enqueue_handle_sweep(pm_handle *h, const SweepArgs &a, int wpl, int wpl_edge)
+{
+    const int lines = lines_of(h, a.dir);
+    return enqueue_sweep_split(h->win, hw_of(h), pl_of(h), wpl, wpl_edge, a, &lines, h->stream, h->side, h->fork,
+                               h->join);
 }
 
 // The whole run: initial depth, initial costs, iterations x 4 sweeps (patchMatch.cu:307-394).
@@ -386,19 +429,21 @@ cudaError_t enqueue_schedule(pm_handle *h)
         const int s_first = h->p.init_mode == PM_INIT_RANDOM ? 1 : 0;
         fill_sweep_args(a, h->d_desc, &lines, 1, d, (uint32_t)k, it == 0 ? s_first : 0, k == nsweeps - 1 ? 1 : 0);
         a.perturb = sweep_perturb(h, k);
-        e = enqueue_sweep(window_side(h), hw_of(h), pl_of(h), h->wpl[orient(d)], a, h->stream);
+        e = enqueue_handle_sweep(h, a, h->wpl[orient(d)], h->wpl_edge[orient(d)]);
         if (e != cudaSuccess) return e;
     }
     return enqueue_final_refine(h, h->d_desc, 0, nsweeps, h->p.init_mode == PM_INIT_RANDOM, h->stream);
 }
 
-// Picks warps per line for both sweep orientations: the caller's choice, a remembered
-// result, or timing candidates on the handle's own buffers (before the run initialises them).
+// Picks warps per line for both sweep orientations, for the interior lines' launch and for the
+// edge lines' one: the caller's choice (both the same), a remembered result, or timing
+// candidates on the handle's own buffers (before the run initialises them): first the interior
+// count with the edge lines at one warp more, then the edge lines' count.
 cudaError_t tune_warps_per_line(pm_handle *h)
 {
     if (h->wpl[0] && h->wpl[1]) return cudaSuccess;
     if (h->p.threads_per_line) {
-        h->wpl[0] = h->wpl[1] = h->p.threads_per_line / 32;
+        h->wpl[0] = h->wpl[1] = h->wpl_edge[0] = h->wpl_edge[1] = h->p.threads_per_line / 32;
         h->stats.threads_per_line = h->p.threads_per_line;
         return cudaSuccess;
     }
@@ -408,7 +453,7 @@ cudaError_t tune_warps_per_line(pm_handle *h)
         const int dir = o == 0 ? PM_DIR_TOP_TO_BOTTOM : PM_DIR_LEFT_TO_RIGHT;
         const TuneKey key{h->device, h->win, h->V, h->p.num_samples, lines_of(h, dir),
                           o == 0 ? h->H : h->W, h->texel_bytes};
-        int best = tuned_lookup(key);
+        int best = tuned_lookup(key);  // interior warps | edge warps << 8
         if (!best) {
             if (!state_ready) {
                 e = launch_init_depth(h->d_desc, 0, h->W * h->H, h->stream);
@@ -416,25 +461,37 @@ cudaError_t tune_warps_per_line(pm_handle *h)
                 if (e != cudaSuccess) return e;
                 state_ready = true;
             }
-            float best_ms = 1e30f;
-            for (int wpl = 1; wpl <= MAX_WARPS_PER_LINE; ++wpl) {
-                SweepArgs a;
-                const int lines = lines_of(h, dir);
-                fill_sweep_args(a, h->d_desc, &lines, 1, dir, 0xFFFFFFF0u, 0, 0);
-                float ms = 0.0f;
-                for (int rep = 0; rep < 2; ++rep) {  // first launch warms caches
-                    e = cudaEventRecord(h->ev[2], h->stream);
-                    if (e == cudaSuccess) e = enqueue_sweep(h->win, hw_of(h), pl_of(h), wpl, a, h->stream);
-                    if (e == cudaSuccess) e = cudaEventRecord(h->ev[3], h->stream);
-                    if (e == cudaSuccess) e = cudaEventSynchronize(h->ev[3]);
-                    if (e != cudaSuccess) return e;
-                    cudaEventElapsedTime(&ms, h->ev[2], h->ev[3]);
+            SweepArgs a;
+            const int lines = lines_of(h, dir);
+            fill_sweep_args(a, h->d_desc, &lines, 1, dir, 0xFFFFFFF0u, 0, 0);
+            auto time_sweep = [&](int wpl, int wpl_edge, float &ms) {
+                cudaError_t r = cudaSuccess;
+                for (int rep = 0; rep < 2 && r == cudaSuccess; ++rep) {  // first launch warms caches
+                    r = cudaEventRecord(h->ev[2], h->stream);
+                    if (r == cudaSuccess) r = enqueue_handle_sweep(h, a, wpl, wpl_edge);
+                    if (r == cudaSuccess) r = cudaEventRecord(h->ev[3], h->stream);
+                    if (r == cudaSuccess) r = cudaEventSynchronize(h->ev[3]);
+                    if (r == cudaSuccess) r = cudaEventElapsedTime(&ms, h->ev[2], h->ev[3]);
                 }
-                if (ms < best_ms) { best_ms = ms; best = wpl; }
+                return r;
+            };
+            float best_ms = 1e30f, ms = 0.0f;
+            int bw = 1, be = 1;
+            for (int wpl = 1; wpl <= MAX_WARPS_PER_LINE; ++wpl) {
+                const int we = std::min(wpl + 1, MAX_WARPS_PER_LINE);
+                if ((e = time_sweep(wpl, we, ms)) != cudaSuccess) return e;
+                if (ms < best_ms) { best_ms = ms; bw = wpl; be = we; }
             }
+            for (int we = bw; we <= MAX_WARPS_PER_LINE; ++we) {
+                if (we == std::min(bw + 1, MAX_WARPS_PER_LINE)) continue;  // timed above
+                if ((e = time_sweep(bw, we, ms)) != cudaSuccess) return e;
+                if (ms < best_ms) { best_ms = ms; be = we; }
+            }
+            best = bw | (be << 8);
             tuned_store(key, best);
         }
-        h->wpl[o] = best;
+        h->wpl[o] = best & 0xFF;
+        h->wpl_edge[o] = best >> 8;
     }
     h->stats.threads_per_line = 32 * std::max(h->wpl[0], h->wpl[1]);
     return cudaSuccess;
@@ -529,8 +586,14 @@ pm_status pm_destroy(pm_handle *h)
         cudaStreamSynchronize(h->stream);
         cudaStreamDestroy(h->stream);
     }
+    if (h->side) {
+        cudaStreamSynchronize(h->side);
+        cudaStreamDestroy(h->side);
+    }
     for (cudaEvent_t e : h->ev)
         if (e) cudaEventDestroy(e);
+    if (h->fork) cudaEventDestroy(h->fork);
+    if (h->join) cudaEventDestroy(h->join);
     if (h->h_sweep_args) cudaFreeHost(h->h_sweep_args);
     delete h;
     return PM_OK;
@@ -684,7 +747,10 @@ pm_status pm_create(const pm_view *views, int n_views, int ref_id, const pm_para
         }                                                                \
     } while (0)
     PM_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    PM_TRY(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
     for (cudaEvent_t &ev : h->ev) PM_TRY(cudaEventCreate(&ev));
+    PM_TRY(cudaEventCreateWithFlags(&h->fork, cudaEventDisableTiming));
+    PM_TRY(cudaEventCreateWithFlags(&h->join, cudaEventDisableTiming));
     PM_TRY(cudaMallocHost((void **)&h->h_sweep_args, sizeof(SweepArgs) * 4 * (size_t)p.num_iterations));
     PM_TRY(cudaEventRecord(h->ev[0], h->stream));
 
@@ -1344,7 +1410,7 @@ pm_status pm_run_sweep(pm_handle *h, int direction, uint32_t sweep_id, int num_s
         PM_CUDA(h, cudaMemcpyAsync(h->d_cost, c.data(), c.size() * 4, cudaMemcpyHostToDevice, h->stream));
     }
     PM_CUDA(h, cudaEventRecord(h->ev[2], h->stream));
-    PM_CUDA(h, enqueue_sweep(h->win, hw_of(h), pl_of(h), h->wpl[orient(direction)], a, h->stream));
+    PM_CUDA(h, enqueue_handle_sweep(h, a, h->wpl[orient(direction)], h->wpl_edge[orient(direction)]));
     PM_CUDA(h, cudaEventRecord(h->ev[3], h->stream));
     PM_CUDA(h, cudaStreamSynchronize(h->stream));
     float ms = 0.0f;

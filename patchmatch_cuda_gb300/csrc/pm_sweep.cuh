@@ -32,8 +32,27 @@ struct SweepArgs {
     int record_views;
     float perturb;                       // > 0: local random search of half-width perturb
     float decay;                         // 2^(-sweep/4): scales the slanted-plane search widths
+    int line_mode;                       // which lines of each reference the blocks take (LineMode)
     int line_start[MAX_BATCH_REFS + 1];  // prefix sums of lines per reference
 };
+
+// The lines of a sweep a launch covers. A line within a half-window of an image edge (its
+// windows cut across the line at every step) does more per step than an interior one, and the
+// sweep lasts as long as its slowest line, so a sweep can run as two concurrent launches: the
+// interior lines, and the edge lines with more warps per line, which the hardware places on the
+// SMs the interior launch leaves room on.
+enum LineMode : int {
+    LINES_ALL = 0,       // lines 0 .. n-1
+    LINES_INTERIOR = 1,  // lines hw .. n-hw-1
+    LINES_EDGES = 2,     // lines 0 .. hw-1 and n-hw .. n-1 (every line when n < 2 hw)
+};
+
+// Lines of a reference a launch in `mode` covers, for a sweep of n lines and half-window hw.
+__host__ __device__ inline int mode_lines(int mode, int n, int hw)
+{
+    const int interior = n > 2 * hw ? n - 2 * hw : 0;
+    return mode == LINES_ALL ? n : mode == LINES_INTERIOR ? interior : n - interior;
+}
 
 __device__ __forceinline__ int find_ref(const SweepArgs &A, int gline)
 {
@@ -140,10 +159,15 @@ __global__ void __maxnreg__(SweepRegs<HW>::value) sweep_kernel(const __grid_cons
     __shared__ float4 s_hh[HH_F4 * MAX_VIEWS];
     stage_ref(A.refs[r], D, s_hh);
     __syncthreads();
-    const int line = gline - A.line_start[r];
     const int Wd = D.width, Hd = D.height, V = D.n_src;
     const int S = A.num_samples > 0 ? A.num_samples : D.num_samples;
     const bool rot = (A.dir == 0 || A.dir == 2);
+    // the block's line: its index among the reference's lines of this launch's mode
+    const int nlines = rot ? Hd : Wd, local = gline - A.line_start[r];
+    const int line = A.line_mode == LINES_INTERIOR ? Window<W>::HW + local
+                     : A.line_mode == LINES_EDGES && local >= min(Window<W>::HW, nlines)
+                         ? nlines - mode_lines(LINES_EDGES, nlines, Window<W>::HW) + local
+                         : local;
     const bool fwd = (A.dir == 0 || A.dir == 1);
     const int axis = rot ? 1 : 0;
     const int nsteps = rot ? Wd : Hd;
@@ -188,7 +212,7 @@ __global__ void __maxnreg__(SweepRegs<HW>::value) sweep_kernel(const __grid_cons
     // line, have a variant of their own); otherwise (a line's first and last half-window of
     // steps) loaded whole
     constexpr int HWIN = Window<W>::HW;
-    const bool cut_line = line < HWIN || line + HWIN >= (rot ? Hd : Wd);
+    const bool cut_line = line < HWIN || line + HWIN >= nlines;
     int ring_step = -1;  // the step whose window the ring holds
     auto load_step = [&](int kk, int xn, int yn) {
         if (rot ? (xn >= HWIN && xn + HWIN < Wd) : (yn >= HWIN && yn + HWIN < Hd)) {
