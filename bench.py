@@ -433,6 +433,7 @@ def run_ours(args):
     e2e_value = total_evals / e2e_max / 1e9
 
     tpl = eng.stats().threads_per_line
+    wpl = list(eng.stats().warps_per_line)
     # variants of the same workload, each one depth map timed once after a warm-up run
     variants = {}
     for name, over in [("f32_texels_box_prefilter", dict(prefilter=1)),
@@ -488,6 +489,8 @@ def run_ours(args):
                 "bad_pixel_pct_0p2pct": round(100 * float(np.mean(rel_err > 0.002)), 3),
                 "median_rel_err_pct": round(100 * float(np.median(rel_err)), 4),
                 "threads_per_line": tpl,
+                "warps_per_line": {"vertical": {"interior": wpl[0], "edge_lines": wpl[1]},
+                                   "horizontal": {"interior": wpl[2], "edge_lines": wpl[3]}},
             },
             "roofline": {
                 "bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",

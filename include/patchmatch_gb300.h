@@ -167,6 +167,8 @@ typedef struct pm_stats {
     float ms_total;                      /* last run                                      */
     int threads_per_line;                /* chosen by the tuner or the caller             */
     int texel_bytes;                     /* 1 (u8), 2 (fp16) or 4 (fp32)                  */
+    int warps_per_line[4];               /* vertical sweeps: interior lines, lines within a
+                                            half-window of an edge; horizontal: the same  */
 } pm_stats;
 
 void pm_default_params(pm_params *p);

@@ -75,6 +75,7 @@ class PmStats(C.Structure):
         ("cost_evals", C.c_ulonglong), ("cost_evals_done", C.c_ulonglong),
         ("ms_prepare", C.c_float), ("ms_init", C.c_float), ("ms_sweeps", C.c_float),
         ("ms_total", C.c_float), ("threads_per_line", C.c_int), ("texel_bytes", C.c_int),
+        ("warps_per_line", C.c_int * 4),
     ]
 
 

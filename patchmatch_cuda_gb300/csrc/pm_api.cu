@@ -437,61 +437,171 @@ cudaError_t enqueue_schedule(pm_handle *h)
 
 // Picks warps per line for both sweep orientations, for the interior lines' launch and for the
 // edge lines' one: the caller's choice (both the same), a remembered result, or timing
-// candidates on the handle's own buffers (before the run initialises them): first the interior
-// count with the edge lines at one warp more, then the edge lines' count.
+// candidates on the handle's own buffers (the run initialises them afterwards). The best count
+// depends on how far the state has converged (early sweeps refresh more views per step), so a
+// candidate is timed from two states, each restored before every trial: the state after the
+// schedule's first iteration and the one after its third, weighted 1 : 3 like the schedule's
+// sweeps after its first iteration. First the interior count with the edge lines at one warp
+// more, then the edge lines' count; near-ties break towards fewer interior and more edge warps.
+// Single sweeps from saved states do not rank near counts as the schedule's sequence of sweeps
+// does, so the picks are then refined on whole iterations.
 cudaError_t tune_warps_per_line(pm_handle *h)
 {
     if (h->wpl[0] && h->wpl[1]) return cudaSuccess;
     if (h->p.threads_per_line) {
         h->wpl[0] = h->wpl[1] = h->wpl_edge[0] = h->wpl_edge[1] = h->p.threads_per_line / 32;
         h->stats.threads_per_line = h->p.threads_per_line;
+        for (int i = 0; i < 4; ++i) h->stats.warps_per_line[i] = h->p.threads_per_line / 32;
         return cudaSuccess;
     }
-    cudaError_t e = cudaSuccess;
-    bool state_ready = false;
+    TuneKey keys[2];
+    int picks[2];
+    bool need = false;
     for (int o = 0; o < 2; ++o) {
         const int dir = o == 0 ? PM_DIR_TOP_TO_BOTTOM : PM_DIR_LEFT_TO_RIGHT;
-        const TuneKey key{h->device, h->win, h->V, h->p.num_samples, lines_of(h, dir),
-                          o == 0 ? h->H : h->W, h->texel_bytes};
-        int best = tuned_lookup(key);  // interior warps | edge warps << 8
-        if (!best) {
-            if (!state_ready) {
-                e = launch_init_depth(h->d_desc, 0, h->W * h->H, h->stream);
-                if (e == cudaSuccess) e = enqueue_costs(h, 1);
-                if (e != cudaSuccess) return e;
-                state_ready = true;
+        keys[o] = TuneKey{h->device, h->win, h->V, h->p.num_samples, lines_of(h, dir), o == 0 ? h->H : h->W,
+                          h->texel_bytes};
+        picks[o] = tuned_lookup(keys[o]);  // interior warps | edge warps << 8
+        need = need || !picks[o];
+    }
+    if (need) {
+        const size_t npix = (size_t)h->W * h->H;
+        const size_t state_floats = npix * (1 + (size_t)h->V) + (pl_of(h) ? 2 * npix : 0);
+        float *snap = nullptr;  // two states
+        cudaError_t e = cudaMallocAsync((void **)&snap, 2 * state_floats * sizeof(float), h->stream);
+        if (e != cudaSuccess) return e;
+        auto copy_state = [&](int which, bool save) {
+            float *parts[3] = {h->d_depth, h->d_cost, (float *)h->d_slopes};
+            const size_t n[3] = {npix, npix * h->V, pl_of(h) ? 2 * npix : 0};
+            size_t off = which * state_floats;
+            cudaError_t r = cudaSuccess;
+            for (int i = 0; i < 3 && r == cudaSuccess; ++i) {
+                if (!n[i]) continue;
+                r = save ? cudaMemcpyAsync(snap + off, parts[i], n[i] * sizeof(float), cudaMemcpyDeviceToDevice, h->stream)
+                         : cudaMemcpyAsync(parts[i], snap + off, n[i] * sizeof(float), cudaMemcpyDeviceToDevice, h->stream);
+                off += n[i];
             }
+            return r;
+        };
+        // the schedule's first three iterations from the initial depth and costs, at a middle
+        // count of warps, with the states after the first and the third kept
+        e = launch_init_depth(h->d_desc, 0, h->W * h->H, h->stream);
+        if (e == cudaSuccess) e = enqueue_costs(h, 1);
+        for (int k = 0; k < 12 && e == cudaSuccess; ++k) {
             SweepArgs a;
+            const int d = k % 4, lines = lines_of(h, d);
+            const int s_first = h->p.init_mode == PM_INIT_RANDOM ? 1 : 0;
+            fill_sweep_args(a, h->d_desc, &lines, 1, d, (uint32_t)k, k < 4 ? s_first : 0, 0);
+            e = enqueue_handle_sweep(h, a, 3, 4);
+            if (e == cudaSuccess && k == 3) e = copy_state(0, true);
+        }
+        if (e == cudaSuccess) e = copy_state(1, true);
+        for (int o = 0; o < 2 && e == cudaSuccess; ++o) {
+            if (picks[o]) continue;
+            const int dir = o == 0 ? PM_DIR_TOP_TO_BOTTOM : PM_DIR_LEFT_TO_RIGHT;
+            SweepArgs a[2];
             const int lines = lines_of(h, dir);
-            fill_sweep_args(a, h->d_desc, &lines, 1, dir, 0xFFFFFFF0u, 0, 0);
-            auto time_sweep = [&](int wpl, int wpl_edge, float &ms) {
+            fill_sweep_args(a[0], h->d_desc, &lines, 1, dir, 4u + (uint32_t)dir, 0, 0);
+            fill_sweep_args(a[1], h->d_desc, &lines, 1, dir, 12u + (uint32_t)dir, 0, 0);
+            // score: the faster of two trials from each state, weighted 1 : 3
+            auto score = [&](int wpl, int wpl_edge, float &out) {
+                out = 0.0f;
                 cudaError_t r = cudaSuccess;
-                for (int rep = 0; rep < 2 && r == cudaSuccess; ++rep) {  // first launch warms caches
-                    r = cudaEventRecord(h->ev[2], h->stream);
-                    if (r == cudaSuccess) r = enqueue_handle_sweep(h, a, wpl, wpl_edge);
-                    if (r == cudaSuccess) r = cudaEventRecord(h->ev[3], h->stream);
-                    if (r == cudaSuccess) r = cudaEventSynchronize(h->ev[3]);
-                    if (r == cudaSuccess) r = cudaEventElapsedTime(&ms, h->ev[2], h->ev[3]);
+                for (int st = 0; st < 2 && r == cudaSuccess; ++st) {
+                    float best_of = 1e30f;
+                    for (int rep = 0; rep < 2 && r == cudaSuccess; ++rep) {
+                        float ms = 0.0f;
+                        r = copy_state(st, false);
+                        if (r == cudaSuccess) r = cudaEventRecord(h->ev[2], h->stream);
+                        if (r == cudaSuccess) r = enqueue_handle_sweep(h, a[st], wpl, wpl_edge);
+                        if (r == cudaSuccess) r = cudaEventRecord(h->ev[3], h->stream);
+                        if (r == cudaSuccess) r = cudaEventSynchronize(h->ev[3]);
+                        if (r == cudaSuccess) r = cudaEventElapsedTime(&ms, h->ev[2], h->ev[3]);
+                        best_of = std::min(best_of, ms);
+                    }
+                    out += (st == 0 ? 1.0f : 3.0f) * best_of;
                 }
                 return r;
             };
-            float best_ms = 1e30f, ms = 0.0f;
-            int bw = 1, be = 1;
-            for (int wpl = 1; wpl <= MAX_WARPS_PER_LINE; ++wpl) {
-                const int we = std::min(wpl + 1, MAX_WARPS_PER_LINE);
-                if ((e = time_sweep(wpl, we, ms)) != cudaSuccess) return e;
-                if (ms < best_ms) { best_ms = ms; bw = wpl; be = we; }
+            // near-ties (within 1 %) go to fewer interior warps, which every SM carries, and to
+            // more warps for the few edge lines, which fit in what the interior launch leaves
+            float sc_int[MAX_WARPS_PER_LINE + 1], sc_edge[MAX_WARPS_PER_LINE + 1];
+            float best = 1e30f;
+            for (int wpl = 1; wpl <= MAX_WARPS_PER_LINE && e == cudaSuccess; ++wpl) {
+                e = score(wpl, std::min(wpl + 1, MAX_WARPS_PER_LINE), sc_int[wpl]);
+                best = std::min(best, sc_int[wpl]);
             }
-            for (int we = bw; we <= MAX_WARPS_PER_LINE; ++we) {
-                if (we == std::min(bw + 1, MAX_WARPS_PER_LINE)) continue;  // timed above
-                if ((e = time_sweep(bw, we, ms)) != cudaSuccess) return e;
-                if (ms < best_ms) { best_ms = ms; be = we; }
+            int bw = 1;
+            while (bw < MAX_WARPS_PER_LINE && sc_int[bw] > 1.01f * best) ++bw;
+            best = 1e30f;
+            for (int we = bw; we <= MAX_WARPS_PER_LINE && e == cudaSuccess; ++we) {
+                if (we == std::min(bw + 1, MAX_WARPS_PER_LINE)) sc_edge[we] = sc_int[bw];  // timed above
+                else e = score(bw, we, sc_edge[we]);
+                best = std::min(best, sc_edge[we]);
             }
-            best = bw | (be << 8);
-            tuned_store(key, best);
+            int be = MAX_WARPS_PER_LINE;
+            while (be > bw && sc_edge[be] > 1.01f * best) --be;
+            picks[o] = bw | (be << 8);
         }
-        h->wpl[o] = best & 0xFF;
-        h->wpl_edge[o] = best >> 8;
+        // the single-sweep picks refined on whole iterations (all four sweeps, both
+        // orientations in the schedule's order, from the two states, weighted 1 : 3): coordinate
+        // descent over the four counts, one count one warp up or down at a time
+        auto iteration_score = [&](const int c[4], float &out) {
+            out = 0.0f;
+            cudaError_t r = cudaSuccess;
+            for (int st = 0; st < 2 && r == cudaSuccess; ++st) {
+                float ms = 0.0f;
+                r = copy_state(st, false);
+                if (r == cudaSuccess) r = cudaEventRecord(h->ev[2], h->stream);
+                for (int d = 0; d < 4 && r == cudaSuccess; ++d) {
+                    SweepArgs a;
+                    const int lines = lines_of(h, d), o = orient(d);
+                    fill_sweep_args(a, h->d_desc, &lines, 1, d, (st == 0 ? 4u : 12u) + (uint32_t)d, 0, 0);
+                    r = enqueue_handle_sweep(h, a, c[2 * o], c[2 * o + 1]);
+                }
+                if (r == cudaSuccess) r = cudaEventRecord(h->ev[3], h->stream);
+                if (r == cudaSuccess) r = cudaEventSynchronize(h->ev[3]);
+                if (r == cudaSuccess) r = cudaEventElapsedTime(&ms, h->ev[2], h->ev[3]);
+                out += (st == 0 ? 1.0f : 3.0f) * ms;
+            }
+            return r;
+        };
+        int cur[4] = {picks[0] & 0xFF, picks[0] >> 8, picks[1] & 0xFF, picks[1] >> 8};
+        float cur_score = 0.0f;
+        if (e == cudaSuccess) e = iteration_score(cur, cur_score);  // warms the caches
+        if (e == cudaSuccess) e = iteration_score(cur, cur_score);
+        for (int pass = 0; pass < 2 && e == cudaSuccess; ++pass) {
+            int best[4] = {cur[0], cur[1], cur[2], cur[3]};
+            float best_score = cur_score;
+            for (int i = 0; i < 4 && e == cudaSuccess; ++i)
+                for (int step = -1; step <= 1 && e == cudaSuccess; step += 2) {
+                    int c[4] = {cur[0], cur[1], cur[2], cur[3]};
+                    c[i] += step;
+                    if (c[i] < 1 || c[i] > MAX_WARPS_PER_LINE) continue;
+                    float sc = 0.0f;
+                    e = iteration_score(c, sc);
+                    if (e == cudaSuccess && sc < 0.995f * best_score) {
+                        best_score = sc;
+                        for (int q = 0; q < 4; ++q) best[q] = c[q];
+                    }
+                }
+            if (std::equal(best, best + 4, cur)) break;
+            for (int q = 0; q < 4; ++q) cur[q] = best[q];
+            cur_score = best_score;
+        }
+        picks[0] = cur[0] | (cur[1] << 8);
+        picks[1] = cur[2] | (cur[3] << 8);
+        if (e == cudaSuccess)
+            for (int o = 0; o < 2; ++o) tuned_store(keys[o], picks[o]);
+        const cudaError_t ef = cudaFreeAsync(snap, h->stream);
+        if (e == cudaSuccess) e = ef;
+        if (e != cudaSuccess) return e;
+    }
+    for (int o = 0; o < 2; ++o) {
+        h->wpl[o] = picks[o] & 0xFF;
+        h->wpl_edge[o] = picks[o] >> 8;
+        h->stats.warps_per_line[2 * o] = h->wpl[o];
+        h->stats.warps_per_line[2 * o + 1] = h->wpl_edge[o];
     }
     h->stats.threads_per_line = 32 * std::max(h->wpl[0], h->wpl[1]);
     return cudaSuccess;
@@ -1083,7 +1193,8 @@ cudaError_t enqueue_batch(pm_batch *b, cudaStream_t s)
 }
 
 // Warps per line for each group and orientation: the fastest of 1 .. MAX_WARPS_PER_LINE on one
-// sweep of the whole group (after its initialisation and initial costs).
+// sweep of the whole group, every trial from the same state (each reference's initialisation
+// and initial costs, restored before each launch; the first of two launches warms the caches).
 cudaError_t tune_batch(pm_batch *b, cudaEvent_t e0, cudaEvent_t e1)
 {
     cudaStream_t s = b->stream;
@@ -1104,29 +1215,57 @@ cudaError_t tune_batch(pm_batch *b, cudaEvent_t e0, cudaEvent_t e1)
             if (e == cudaSuccess) e = launch_window(h->win, hw_of(h), pl_of(h), req);
         }
         if (e != cudaSuccess) return e;
-        for (int o = 0; o < 2; ++o) {
+        // snapshot of every reference's depth, costs and (slanted planes) slopes
+        std::vector<std::pair<void *, size_t>> parts;
+        for (pm_handle *h : g.refs) {
+            const size_t npix = (size_t)h->W * h->H;
+            parts.push_back({h->d_depth, npix * sizeof(float)});
+            parts.push_back({h->d_cost, npix * h->V * sizeof(float)});
+            if (g.pl) parts.push_back({h->d_slopes, npix * sizeof(float2)});
+        }
+        size_t total = 0;
+        for (auto &pt : parts) total += pt.second;
+        char *snap = nullptr;
+        e = cudaMallocAsync((void **)&snap, total, s);
+        if (e != cudaSuccess) return e;
+        auto copy_state = [&](bool save) {
+            size_t off = 0;
+            cudaError_t r = cudaSuccess;
+            for (auto &pt : parts) {
+                if (r == cudaSuccess)
+                    r = save ? cudaMemcpyAsync(snap + off, pt.first, pt.second, cudaMemcpyDeviceToDevice, s)
+                             : cudaMemcpyAsync(pt.first, snap + off, pt.second, cudaMemcpyDeviceToDevice, s);
+                off += pt.second;
+            }
+            return r;
+        };
+        e = copy_state(true);
+        for (int o = 0; o < 2 && e == cudaSuccess; ++o) {
             const int d = o == 0 ? PM_DIR_TOP_TO_BOTTOM : PM_DIR_LEFT_TO_RIGHT;
             std::vector<int> lines;
             for (pm_handle *h : g.refs) lines.push_back(lines_of(h, d));
             float best_ms = 1e30f;
-            for (int wpl = 1; wpl <= MAX_WARPS_PER_LINE; ++wpl) {
+            for (int wpl = 1; wpl <= MAX_WARPS_PER_LINE && e == cudaSuccess; ++wpl) {
                 SweepArgs a;
                 fill_sweep_args(a, g.d_descs, lines.data(), m, d, 0xFFFFFFF0u, 0, 0);
                 float ms = 0.0f;
-                for (int rep = 0; rep < 2; ++rep) {  // the first launch warms the caches
-                    e = cudaEventRecord(e0, s);
+                for (int rep = 0; rep < 2 && e == cudaSuccess; ++rep) {
+                    e = copy_state(false);
+                    if (e == cudaSuccess) e = cudaEventRecord(e0, s);
                     if (e == cudaSuccess) e = enqueue_sweep(g.win, g.hw, g.pl, wpl, a, s);
                     if (e == cudaSuccess) e = cudaEventRecord(e1, s);
                     if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-                    if (e != cudaSuccess) return e;
-                    cudaEventElapsedTime(&ms, e0, e1);
+                    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
                 }
-                if (ms < best_ms) {
+                if (e == cudaSuccess && ms < best_ms) {
                     best_ms = ms;
                     g.wpl[o] = wpl;
                 }
             }
         }
+        const cudaError_t ef = cudaFreeAsync(snap, s);
+        if (e == cudaSuccess) e = ef;
+        if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
 }

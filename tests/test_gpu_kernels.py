@@ -205,15 +205,18 @@ def test_philox_matches_oracle(engine_lib):
         np.testing.assert_array_equal(out[i], pm_oracle.philox(ctr[i], key))
 
 
-@pytest.mark.parametrize("exp_shift", [-20, -3, 0, 5, 11])
-def test_newton_reciprocal_is_correctly_rounded(engine_lib, exp_shift):
-    """The texture-filtering sampler's 1/z (hardware approximation + two Newton corrections)
-    equals the correctly rounded reciprocal for every significand of the binade, both signs:
+def test_newton_reciprocal_is_correctly_rounded(engine_lib):
+    """The samplers' 1/z (hardware approximation + one Newton correction) equals the correctly
+    rounded reciprocal for every significand, both signs, of every binade from 2^-120 to 2^120:
     the oracle's single-precision coordinates rest on that."""
     import ctypes as C
-    bad = C.c_ulonglong(0)
-    assert engine_lib.pm_check_reciprocal(exp_shift, C.byref(bad)) == 0
-    assert bad.value == 0
+    failing = []
+    for exp_shift in range(-120, 121):
+        bad = C.c_ulonglong(0)
+        assert engine_lib.pm_check_reciprocal(exp_shift, C.byref(bad)) == 0
+        if bad.value:
+            failing.append((exp_shift, bad.value))
+    assert not failing, failing
 
 
 def test_initial_depth_and_costs_match_oracle(small_scene, parity_log):
