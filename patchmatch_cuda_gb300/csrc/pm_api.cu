@@ -7,6 +7,7 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -344,12 +345,14 @@ cudaError_t enqueue_sweep_split(int win, bool hw, bool pl, int wpl, int wpl_edge
 // A line's steps are sequential, so a sweep takes ceil(lines / resident lines) line-times;
 // more warps per line shorten a line-time but fit fewer lines. The tuner times one sweep
 // of the real workload for each candidate and remembers the winner per shape.
+// A shape the tuner remembers: the kernel (window, sampler, plane mode) and the work per sweep.
 struct TuneKey {
     int device, win, n_src, num_samples, lines, steps, texel_bytes;
+    bool hw, pl;
     bool operator==(const TuneKey &o) const
     {
         return device == o.device && win == o.win && n_src == o.n_src && num_samples == o.num_samples &&
-               lines == o.lines && steps == o.steps && texel_bytes == o.texel_bytes;
+               lines == o.lines && steps == o.steps && texel_bytes == o.texel_bytes && hw == o.hw && pl == o.pl;
     }
 };
 std::mutex g_tune_mutex;
@@ -437,14 +440,12 @@ cudaError_t enqueue_schedule(pm_handle *h)
 
 // Picks warps per line for both sweep orientations, for the interior lines' launch and for the
 // edge lines' one: the caller's choice (both the same), a remembered result, or timing
-// candidates on the handle's own buffers (the run initialises them afterwards). The best count
-// depends on how far the state has converged (early sweeps refresh more views per step), so a
-// candidate is timed from two states, each restored before every trial: the state after the
+// candidates on the handle's own buffers (the run initialises them afterwards). The best counts
+// depend on how far the state has converged (early sweeps refresh more views per step), so
+// candidates are timed from two states, each restored before every trial: the state after the
 // schedule's first iteration and the one after its third, weighted 1 : 3 like the schedule's
-// sweeps after its first iteration. First the interior count with the edge lines at one warp
-// more, then the edge lines' count; near-ties break towards fewer interior and more edge warps.
-// Single sweeps from saved states do not rank near counts as the schedule's sequence of sweeps
-// does, so the picks are then refined on whole iterations.
+// sweeps after its first iteration. Every pair of counts is timed on single sweeps; the pairs
+// near the best are then timed on whole iterations.
 cudaError_t tune_warps_per_line(pm_handle *h)
 {
     if (h->wpl[0] && h->wpl[1]) return cudaSuccess;
@@ -460,7 +461,7 @@ cudaError_t tune_warps_per_line(pm_handle *h)
     for (int o = 0; o < 2; ++o) {
         const int dir = o == 0 ? PM_DIR_TOP_TO_BOTTOM : PM_DIR_LEFT_TO_RIGHT;
         keys[o] = TuneKey{h->device, h->win, h->V, h->p.num_samples, lines_of(h, dir), o == 0 ? h->H : h->W,
-                          h->texel_bytes};
+                          h->texel_bytes, hw_of(h), pl_of(h)};
         picks[o] = tuned_lookup(keys[o]);  // interior warps | edge warps << 8
         need = need || !picks[o];
     }
@@ -496,8 +497,12 @@ cudaError_t tune_warps_per_line(pm_handle *h)
             if (e == cudaSuccess && k == 3) e = copy_state(0, true);
         }
         if (e == cudaSuccess) e = copy_state(1, true);
+        std::vector<int> cand[2];  // each orientation's candidate pairs (interior | edge << 8)
         for (int o = 0; o < 2 && e == cudaSuccess; ++o) {
-            if (picks[o]) continue;
+            if (picks[o]) {
+                cand[o].push_back(picks[o]);
+                continue;
+            }
             const int dir = o == 0 ? PM_DIR_TOP_TO_BOTTOM : PM_DIR_LEFT_TO_RIGHT;
             SweepArgs a[2];
             const int lines = lines_of(h, dir);
@@ -523,29 +528,25 @@ cudaError_t tune_warps_per_line(pm_handle *h)
                 }
                 return r;
             };
-            // near-ties (within 1 %) go to fewer interior warps, which every SM carries, and to
-            // more warps for the few edge lines, which fit in what the interior launch leaves
-            float sc_int[MAX_WARPS_PER_LINE + 1], sc_edge[MAX_WARPS_PER_LINE + 1];
-            float best = 1e30f;
-            for (int wpl = 1; wpl <= MAX_WARPS_PER_LINE && e == cudaSuccess; ++wpl) {
-                e = score(wpl, std::min(wpl + 1, MAX_WARPS_PER_LINE), sc_int[wpl]);
-                best = std::min(best, sc_int[wpl]);
-            }
-            int bw = 1;
-            while (bw < MAX_WARPS_PER_LINE && sc_int[bw] > 1.01f * best) ++bw;
-            best = 1e30f;
-            for (int we = bw; we <= MAX_WARPS_PER_LINE && e == cudaSuccess; ++we) {
-                if (we == std::min(bw + 1, MAX_WARPS_PER_LINE)) sc_edge[we] = sc_int[bw];  // timed above
-                else e = score(bw, we, sc_edge[we]);
-                best = std::min(best, sc_edge[we]);
-            }
-            int be = MAX_WARPS_PER_LINE;
-            while (be > bw && sc_edge[be] > 1.01f * best) --be;
-            picks[o] = bw | (be << 8);
+            // every pair (interior warps, edge-line warps = interior .. interior + 2): the best
+            // counts of the two launches depend on each other (how much room the interior launch
+            // leaves decides where the edge blocks fit)
+            std::vector<std::pair<float, int>> pairs;
+            for (int wpl = 1; wpl <= MAX_WARPS_PER_LINE && e == cudaSuccess; ++wpl)
+                for (int we = wpl; we <= std::min(wpl + 2, MAX_WARPS_PER_LINE) && e == cudaSuccess; ++we) {
+                    float sc = 0.0f;
+                    e = score(wpl, we, sc);
+                    pairs.push_back({sc, wpl | (we << 8)});
+                }
+            std::sort(pairs.begin(), pairs.end());
+            for (auto &pr : pairs)
+                if (cand[o].size() < 8 && pr.first <= 1.10f * pairs.front().first) cand[o].push_back(pr.second);
         }
-        // the single-sweep picks refined on whole iterations (all four sweeps, both
-        // orientations in the schedule's order, from the two states, weighted 1 : 3): coordinate
-        // descent over the four counts, one count one warp up or down at a time
+        // single sweeps from saved states do not rank near pairs as the schedule's sequence of
+        // sweeps does: each orientation's candidates (its pairs within 10 % of the best single-
+        // sweep score, at most 8) are timed on whole iterations (all four sweeps in the
+        // schedule's order, from both states, weighted 1 : 3), the other orientation at its best
+        // single-sweep pair; the fastest wins, a pair within 0.5 % of it with fewer warps first
         auto iteration_score = [&](const int c[4], float &out) {
             out = 0.0f;
             cudaError_t r = cudaSuccess;
@@ -566,31 +567,31 @@ cudaError_t tune_warps_per_line(pm_handle *h)
             }
             return r;
         };
-        int cur[4] = {picks[0] & 0xFF, picks[0] >> 8, picks[1] & 0xFF, picks[1] >> 8};
-        float cur_score = 0.0f;
-        if (e == cudaSuccess) e = iteration_score(cur, cur_score);  // warms the caches
-        if (e == cudaSuccess) e = iteration_score(cur, cur_score);
-        for (int pass = 0; pass < 2 && e == cudaSuccess; ++pass) {
-            int best[4] = {cur[0], cur[1], cur[2], cur[3]};
-            float best_score = cur_score;
-            for (int i = 0; i < 4 && e == cudaSuccess; ++i)
-                for (int step = -1; step <= 1 && e == cudaSuccess; step += 2) {
-                    int c[4] = {cur[0], cur[1], cur[2], cur[3]};
-                    c[i] += step;
-                    if (c[i] < 1 || c[i] > MAX_WARPS_PER_LINE) continue;
-                    float sc = 0.0f;
-                    e = iteration_score(c, sc);
-                    if (e == cudaSuccess && sc < 0.995f * best_score) {
-                        best_score = sc;
-                        for (int q = 0; q < 4; ++q) best[q] = c[q];
-                    }
-                }
-            if (std::equal(best, best + 4, cur)) break;
-            for (int q = 0; q < 4; ++q) cur[q] = best[q];
-            cur_score = best_score;
+        int chosen[2] = {cand[0].empty() ? 0 : cand[0][0], cand[1].empty() ? 0 : cand[1][0]};
+        bool warmed = false;
+        for (int o = 0; o < 2 && e == cudaSuccess; ++o) {
+            if (cand[o].size() < 2) continue;
+            std::vector<std::pair<float, int>> scored;
+            for (int pr : cand[o]) {
+                int c[4] = {chosen[0] & 0xFF, chosen[0] >> 8, chosen[1] & 0xFF, chosen[1] >> 8};
+                c[2 * o] = pr & 0xFF;
+                c[2 * o + 1] = pr >> 8;
+                float sc = 0.0f;
+                if (!warmed) { e = iteration_score(c, sc); warmed = true; }  // warms the caches
+                if (e == cudaSuccess) e = iteration_score(c, sc);
+                if (e != cudaSuccess) break;
+                scored.push_back({sc, pr});
+            }
+            if (e != cudaSuccess) break;
+            float best = 1e30f;
+            for (auto &x : scored) best = std::min(best, x.first);
+            int fewest = 1 << 30;
+            for (auto &x : scored) {
+                const int warps = (x.second & 0xFF) + (x.second >> 8);
+                if (x.first <= 1.005f * best && warps < fewest) { fewest = warps; chosen[o] = x.second; }
+            }
         }
-        picks[0] = cur[0] | (cur[1] << 8);
-        picks[1] = cur[2] | (cur[3] << 8);
+        if (e == cudaSuccess) { picks[0] = chosen[0]; picks[1] = chosen[1]; }
         if (e == cudaSuccess)
             for (int o = 0; o < 2; ++o) tuned_store(keys[o], picks[o]);
         const cudaError_t ef = cudaFreeAsync(snap, h->stream);
@@ -1539,14 +1540,24 @@ pm_status pm_run_sweep(pm_handle *h, int direction, uint32_t sweep_id, int num_s
     a.perturb = sweep_perturb(h, (int)sweep_id);
     if (record_views && num_samples > h->p.num_samples) return PM_ERR_INVALID_ARGUMENT;
     if (!h->wpl[orient(direction)]) {
-        // tune on scratch copies so the caller's state is untouched
-        std::vector<float> d((size_t)h->W * h->H), c((size_t)h->W * h->H * h->V);
+        // the tuner sweeps the handle's own buffers: keep the caller's state (depth, costs and,
+        // with slanted planes, the slopes) and put it back afterwards
+        const size_t npix = (size_t)h->W * h->H;
+        std::vector<float> d(npix), c(npix * h->V);
+        std::vector<float2> sl(pl_of(h) ? npix : 0);
         PM_CUDA(h, cudaMemcpyAsync(d.data(), h->d_depth, d.size() * 4, cudaMemcpyDeviceToHost, h->stream));
         PM_CUDA(h, cudaMemcpyAsync(c.data(), h->d_cost, c.size() * 4, cudaMemcpyDeviceToHost, h->stream));
+        if (!sl.empty())
+            PM_CUDA(h, cudaMemcpyAsync(sl.data(), h->d_slopes, sl.size() * sizeof(float2), cudaMemcpyDeviceToHost,
+                                       h->stream));
         PM_CUDA(h, cudaStreamSynchronize(h->stream));
         PM_CUDA(h, tune_warps_per_line(h));
         PM_CUDA(h, cudaMemcpyAsync(h->d_depth, d.data(), d.size() * 4, cudaMemcpyHostToDevice, h->stream));
         PM_CUDA(h, cudaMemcpyAsync(h->d_cost, c.data(), c.size() * 4, cudaMemcpyHostToDevice, h->stream));
+        if (!sl.empty())
+            PM_CUDA(h, cudaMemcpyAsync(h->d_slopes, sl.data(), sl.size() * sizeof(float2), cudaMemcpyHostToDevice,
+                                       h->stream));
+        PM_CUDA(h, cudaStreamSynchronize(h->stream));  // the host copies must outlive the transfers
     }
     PM_CUDA(h, cudaEventRecord(h->ev[2], h->stream));
     PM_CUDA(h, enqueue_handle_sweep(h, a, h->wpl[orient(direction)], h->wpl_edge[orient(direction)]));

@@ -16,10 +16,12 @@ namespace pm {
 
 constexpr int MAX_BATCH_REFS = 256;
 constexpr int MAX_WARPS_PER_LINE = 6;
-// Register caps of the sweep kernel: 72 per thread with the texture-filtering sampler (nine
-// 3-warp lines or five 5-warp lines resident per SM); 96 with the exact sampler, whose
-// gathers hold four texels.
-template <bool HW> struct SweepRegs { static constexpr int value = HW ? 72 : 96; };
+// Register caps of the sweep kernel: 72 per thread with the texture-filtering sampler up to a
+// 16-column window (the half-warp layout: nine 3-warp lines resident per SM), 96 for wider
+// windows (the whole-warp layout's fully unrolled column holds more samples in flight: at 72
+// the 19x19 kernel spilled 420 bytes, and the 8 x 3072x2048 batch took 13.4 s against 12.4 s
+// at 96 and 12.9 s at 128); 96 with the exact sampler, whose gathers hold four texels.
+template <int W, bool HW> struct SweepRegs { static constexpr int value = HW ? (W > 16 ? 96 : 72) : 96; };
 constexpr int COST_BLOCK = 128;
 
 struct SweepArgs {
@@ -147,7 +149,7 @@ __device__ __forceinline__ void make_draws(const RefDesc &D, uint32_t pix, uint3
 //              views' NCCs at the chosen depth, two views per pass;
 //   after B3   warp 0 commits the costs, the depth and the forward message.
 template <int W, bool HW, bool PL>
-__global__ void __maxnreg__(SweepRegs<HW>::value) sweep_kernel(const __grid_constant__ SweepArgs A)
+__global__ void __maxnreg__((SweepRegs<W, HW>::value)) sweep_kernel(const __grid_constant__ SweepArgs A)
 {
     constexpr int TAB = Window<W>::TAB;
     const int lane = threadIdx.x & 31;
