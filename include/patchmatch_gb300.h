@@ -115,7 +115,8 @@ typedef struct pm_params {
     uint64_t seed;                 /* Philox key                                             */
     int precision;                 /* pm_precision                                           */
     int init_mode;                 /* pm_init_mode                                           */
-    int threads_per_line;          /* 0 = tuned; else 32, 64 or 128                          */
+    int threads_per_line;          /* 0 = tuned; else a multiple of 32 up to 192, for both
+                                      launches of every sweep                                */
     int quirks;                    /* 1 (default): keep the reference's leading-edge window
                                       misalignment (patchMatch.cu:546); 0: aligned windows   */
     int gpu_id;                    /* gpuId: -1 = current device (main.cpp:56-59)            */

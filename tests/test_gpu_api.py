@@ -50,6 +50,25 @@ def test_depth_outputs_file_format_and_view_selection(small, tmp_path):
     eng.close()
 
 
+def test_warps_per_line_reported(small):
+    """The tuner's counts (vertical interior, vertical edge lines, horizontal interior, horizontal
+    edge lines) are reported in the stats; a caller's threads_per_line sets all four, and the
+    depth map does not depend on them."""
+    tuned = _engine(small)
+    tuned.run()
+    st = tuned.stats()
+    wpl = list(st.warps_per_line)
+    assert all(1 <= w <= 6 for w in wpl), wpl
+    assert st.threads_per_line == 32 * max(wpl[0], wpl[2])
+    fixed = _engine(small, threads_per_line=64)
+    fixed.run()
+    assert list(fixed.stats().warps_per_line) == [2, 2, 2, 2]
+    np.testing.assert_array_equal(fixed.depth(), tuned.depth())
+    np.testing.assert_array_equal(fixed.view_selection(), tuned.view_selection())
+    tuned.close()
+    fixed.close()
+
+
 def test_runs_are_deterministic_and_async_matches_sync(small):
     eng = _engine(small)
     eng.run()
