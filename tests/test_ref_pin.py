@@ -322,3 +322,39 @@ def test_blur_against_reference(shape, oracle_lib):
         assert kw == kw64 == taps
         np.testing.assert_array_equal(pm_oracle.prefilter(img, 1, sigma, fp32=True), r32.astype(np.float32))
         assert np.abs(pm_oracle.prefilter(img, 1, sigma) - r64).max() <= 6e-8
+
+
+@needs_reference
+@pytest.mark.parametrize("half_window", [1, 4, 9, 11])
+def test_window_sums_and_ncc_against_reference_at_other_windows(golden, half_window, oracle_lib, parity_log):
+    """The reference instantiates its kernels for every odd window (PatchMatch::run<W>,
+    patchMatch.cu:276-296); the fixture holds its 15x15 outputs. At other windows, on the
+    fixture's views: the window sums of the widened build equal the oracle's, and computeNCC
+    (patchMatch.cu:433-611) agrees to FP64 rounding on queries at every border and inside
+    (1e-11: a 3x3 window's nine samples make the NCC far worse conditioned than 15x15's)."""
+    from oracle import pm_oracle, pm_ref
+    p = G.params()
+    p.half_window = half_window
+    views = G.stored_views(golden)
+    ref_id = int(golden["ref_id"])
+    rp = pm_ref.RefProblem.from_images(views, ref_id, p, wide=True, fixed_point_weights=False)
+    orc = pm_oracle.from_images(views, ref_id, p)
+    _, si, sii = rp.box_moments()
+    np.testing.assert_array_equal(orc.sum_i, si)
+    np.testing.assert_array_equal(orc.sum_ii, sii)
+    w = G.WORKLOAD
+    rng = np.random.default_rng(100 + half_window)
+    n = 512
+    xs, ys = rng.integers(0, w.width, n), rng.integers(0, w.height, n)
+    xs[:64] = rng.integers(0, half_window + 1, 64)
+    ys[64:128] = rng.integers(0, half_window + 1, 64)
+    xs[128:192] = rng.integers(w.width - half_window - 1, w.width, 64)
+    ys[192:256] = rng.integers(w.height - half_window - 1, w.height, 64)
+    vs = rng.integers(0, w.n_src, n)
+    ds = rng.uniform(w.depth_near, w.depth_far, n).astype(np.float32).astype(np.float64)
+    ax = rng.integers(0, 2, n)
+    want = rp.ncc(xs, ys, vs, ds, ax)
+    got = orc.ncc_batch(xs.astype(np.int32), ys.astype(np.int32), vs.astype(np.int32), ds, ax.astype(np.int32))
+    err = rel_err(got, want)
+    parity_log(f"ref_pin_ncc_half_window{half_window}", n=n, err_max=float(err.max()))
+    assert err.max() <= 1e-11
