@@ -358,3 +358,47 @@ def test_window_sums_and_ncc_against_reference_at_other_windows(golden, half_win
     err = rel_err(got, want)
     parity_log(f"ref_pin_ncc_half_window{half_window}", n=n, err_max=float(err.max()))
     assert err.max() <= 1e-11
+
+
+@needs_reference
+@pytest.mark.parametrize("half_window", [4, 9])
+def test_sweeps_against_reference_at_other_windows(golden, half_window, oracle_lib, parity_log):
+    """topToDown / downToTop (patchMatch.cu:818-1209) at windows other than the fixture's:
+    every line of one sweep per direction with S = 5, the widened build and the oracle each from
+    the oracle's initial depth and costs with the same random streams; every decision equal up
+    to a line's first step whose posterior CDF is NaN (where the widened build has no float
+    underflow)."""
+    from oracle import pm_oracle, pm_ref
+    p = G.params()
+    p.half_window = half_window
+    views = G.stored_views(golden)
+    ref_id = int(golden["ref_id"])
+    rp = pm_ref.RefProblem.from_images(views, ref_id, p, wide=True, fixed_point_weights=False)
+    orc = pm_oracle.from_images(views, ref_id, p)
+    w = G.WORKLOAD
+    counts0 = np.zeros(golden["counts0"].shape, np.uint32)
+    orc.set_stream(counts0)
+    try:
+        d0 = orc.init_depth()
+        c0 = orc.initial_costs(d0)
+        events = decisions = cut = 0
+        for direction in range(4):
+            rd, rc, rcount = d0.copy(), c0.copy(), counts0.copy()
+            rp.sweep(rd, rc, rcount, direction, S)
+            od, oc, ocount = d0.copy(), c0.copy(), counts0.copy()
+            vs = np.full((S, w.height, w.width), 255, np.uint8)
+            orc.set_stream(ocount)
+            orc.sweep(od, oc, direction, 4 + direction, S, view_sel=vs)
+            prefix, nsteps = first_divergence(rd, od, direction)
+            rows = np.moveaxis(vs, 0, -1) if direction in (0, 2) else np.moveaxis(vs, 0, -1).swapaxes(0, 1)
+            rows = rows[:, ::-1] if direction in (2, 3) else rows
+            limit = _undefined_prefix(rows, nsteps)
+            events += int(np.sum((prefix < nsteps) & (prefix < limit)))
+            ev, dec = divergence_stats(np.minimum(prefix, limit), nsteps)
+            decisions += dec
+            cut += int(np.sum(limit < nsteps))
+    finally:
+        orc.set_stream(None)
+    parity_log(f"ref_pin_sweeps_half_window{half_window}", divergences=events, decisions=decisions,
+               lines_cut_at_nan_cdf=cut)
+    assert decisions > 0 and events == 0, f"{events} decisions differ from the widened reference"
