@@ -174,6 +174,10 @@ typedef struct pm_stats {
 
 void pm_default_params(pm_params *p);
 const char *pm_status_string(pm_status s);
+/* The sizes of the public structs as this library was built, in the order pm_view, pm_params,
+ * pm_stats, pm_fuse_params, pm_depth_view: the first n of them into out. Lets a binding check
+ * its mirrors of the structs before it passes one. Returns how many it wrote. */
+int pm_struct_sizes(size_t *out, int n);
 const char *pm_last_error(const pm_handle *h);
 
 /* Validates, sets up cameras (K^-1, C, H1, H2 in FP64), uploads and prefilters the images,

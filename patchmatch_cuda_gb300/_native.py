@@ -42,7 +42,7 @@ EXPORTED_SYMBOLS = [
     "pm_fusion_create", "pm_fusion_create_from_engines", "pm_fusion_run", "pm_fusion_info",
     "pm_fusion_get_points", "pm_fusion_get_depth", "pm_fusion_geometry", "pm_fusion_write_ply",
     "pm_fusion_last_error", "pm_fusion_destroy", "pm_refine", "pm_get_slopes", "pm_set_slopes",
-    "pm_get_normals", "pm_eval_costs_planes",
+    "pm_get_normals", "pm_eval_costs_planes", "pm_struct_sizes",
 ]
 
 MAX_FUSE_REFS = 256
@@ -143,6 +143,7 @@ def load_engine() -> C.CDLL:
         "pm_transpose_layers": (C.c_int, [P, C.c_size_t, P, C.c_size_t, C.c_int, C.c_int, C.c_int, P]),
         "pm_philox": (C.c_int, [C.c_uint64, C.c_int, P, P]),
         "pm_check_reciprocal": (C.c_int, [C.c_int, P]),
+        "pm_struct_sizes": (C.c_int, [P, C.c_int]),
         "pm_gemm_bf16": (C.c_int, [P, C.c_int, P, C.c_int, C.c_int, C.c_int, C.c_int, P, C.c_int, C.c_int, P,
                                    C.c_int, C.c_int, P]),
         "pm_gemm_error": (C.c_int, [P, C.c_int]),

@@ -667,6 +667,17 @@ void pm_default_params(pm_params *p)
     p->block_dim_y = 16;
 }
 
+int pm_struct_sizes(size_t *out, int n)
+{
+    const size_t sizes[] = {sizeof(pm_view), sizeof(pm_params), sizeof(pm_stats), sizeof(pm_fuse_params),
+                            sizeof(pm_depth_view)};
+    const int total = (int)(sizeof sizes / sizeof sizes[0]);
+    if (!out || n <= 0) return 0;
+    const int k = n < total ? n : total;
+    for (int i = 0; i < k; ++i) out[i] = sizes[i];
+    return k;
+}
+
 const char *pm_status_string(pm_status s)
 {
     const int i = (int)s;

@@ -128,3 +128,14 @@ def test_fusion_arguments_are_checked_before_the_device(engine_lib):
     lib.pm_default_fuse_params(C.byref(p))
     assert (p.max_reproj_px, round(p.max_rel_depth, 6), p.min_consistent) == (1.0, 0.01, 2)
 
+
+
+def test_struct_mirrors_match_the_library(engine_lib):
+    """The ctypes mirrors of the public structs have the library's sizes (a mirror that is too
+    small would let pm_get_stats or pm_create read or write past it)."""
+    import ctypes as C
+    from patchmatch_cuda_gb300 import _native
+    sizes = (C.c_size_t * 5)()
+    assert engine_lib.pm_struct_sizes(sizes, 5) == 5
+    mirrors = [_native.PmView, _native.PmParams, _native.PmStats, _native.PmFuseParams, _native.PmDepthView]
+    assert [C.sizeof(m) for m in mirrors] == list(sizes)
