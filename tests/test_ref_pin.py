@@ -402,3 +402,35 @@ def test_sweeps_against_reference_at_other_windows(golden, half_window, oracle_l
     parity_log(f"ref_pin_sweeps_half_window{half_window}", divergences=events, decisions=decisions,
                lines_cut_at_nan_cdf=cut)
     assert decisions > 0 and events == 0, f"{events} decisions differ from the widened reference"
+
+
+@needs_reference
+@pytest.mark.parametrize("n_views", [1, 2, 20, 32])
+def test_messages_against_reference_at_other_view_counts(n_views, oracle_lib):
+    """computeMessageForward / computeMessageBackward (patchMatch.cu:669-715) for view counts
+    other than the fixture's 10, up to the 32 a warp's lanes hold, and three SPMAlpha values:
+    the oracle's messages and replacement-draw counts equal the widened build's."""
+    from oracle import pm_oracle, pm_ref
+    rng = np.random.default_rng(n_views)
+    n = 24
+    msg = rng.uniform(0.0, 1.0, (n, n_views))
+    cost = rng.uniform(0.0, 2.0, (n, n_views))
+    cost[rng.random((n, n_views)) < 0.15] = 2.0      # the cost-2 replacement draws
+    cost[:4] = rng.uniform(2.0, 12.0, (4, n_views))   # leading-edge values beyond [0, 2]
+    msg[4:8] = rng.choice([0.0, 1.0, 0.5], (4, n_views))
+    seed = 2024
+    for sp_alpha in (0.2, 0.45, 1.0):
+        for fwd in (True, False):
+            f = pm_oracle.msg_forward if fwd else pm_oracle.msg_backward
+            for i in range(n):
+                want, draws = pm_ref.messages(fwd, msg[i], cost[i], sp_alpha, seed, 1000 + i, 0, wide=True)
+                k = 0
+                got = np.empty(n_views)
+                for v in range(n_views):
+                    u = 0.0
+                    if cost[i, v] == 2.0:
+                        u = pm_oracle.load().pmo_uniform(seed, 1000 + i, k, 0x5EED << 16, 0)
+                        k += 1
+                    got[v] = f(msg[i, v], cost[i, v], u, sp_alpha)
+                assert k == draws
+                np.testing.assert_allclose(got, want, rtol=1e-7, atol=1e-12)
